@@ -1,0 +1,170 @@
+/*
+ * unap_cuda.h -- C ABI of the GB300 UNAP solve library (libunap_cuda.so).
+ *
+ * Part 1 re-exports the reference's Fortran-callable interface with the same
+ * symbol names, argument order and meaning, so a Fortran/C caller of
+ * UNAP's src/tools/cInterface/fortranInterface.h relinks against this library
+ * unchanged.  Conventions kept from the reference:
+ *   - every argument is passed by pointer; labels are 32-bit `int`
+ *     (the C header fortranInterface.h:8-102 uses int*);
+ *   - handles are C pointers stored in a `long int` the caller owns;
+ *   - one-shot solves (pcgsolversolve_, pbicgstabsolversolve_,
+ *     mgsolversolve_) copy x/b in and out and DELETE the matrix handle they
+ *     were given (fortranInterface.cpp:267,345,463);
+ *   - preconditioner codes 1 Diag, 2 DIC, 3 DILU, anything else none;
+ *     smoother codes 1 Gauss-Seidel, 2 Chebyshev;
+ *   - a matrix is symmetric iff the `lower` and `upper` pointers are equal.
+ * Differences, all documented at the declaration:
+ *   - ldumatrixcreat_ builds an asymmetric matrix from separate lower/upper
+ *     arrays (the reference overwrites upper with lower,
+ *     fortranInterface.cpp:51-58);
+ *   - errors do not exit(): the solve reports num_iterations = -1 and
+ *     final_res_norm = NaN and the message is kept for unap_cuda_last_error().
+ *   - processor interfaces (MPI halos) are accepted and ignored: one GPU is
+ *     one rank, and the reference ignores interfaces on a single rank
+ *     (lduMatrix.cpp:488-503, PARRUN false).
+ *
+ * Part 2 adds unap_cuda_* entry points that have no counterpart in the
+ * reference: device-pointer solves and kernels, AMG-PCG in FP64 and mixed
+ * precision, batched and served solves.  They return 0 on success and a
+ * negative code on error.
+ */
+#ifndef UNAP_CUDA_H
+#define UNAP_CUDA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ===================================================================== */
+/* Part 1: the reference's Fortran-convention interface                  */
+/* ===================================================================== */
+
+/* fortranInterface.h:8-18 / fortranInterface.cpp:31-71.
+ * 0-based addresses; faces should be oriented lowerAddr < upperAddr and sorted
+ * by owner for DIC/DILU/Gauss-Seidel (SpMV accepts any order). */
+void ldumatrixcreat_(long int* APtrPtr, int* nCells, int* upperSize, int* lowerAddr,
+                     int* upperAddr, double* lower, double* diag, double* upper);
+
+/* fortranInterface.h:20-29 / fortranInterface.cpp:74-120.  1-based COO rows
+ * and columns, rows sorted; the structure must be symmetric.  symm != 0 means
+ * the values are symmetric. */
+void coo2ldumatrixcreat_(long int* APtrPtr, const double* dataPtr, const int* rowsPtr,
+                         const int* columnPtr, const int* nCells, const int* size,
+                         const int* symm);
+
+/* fortranInterface.h:32-41 / fortranInterface.cpp:123-146.  Compressed rows
+ * with sorted columns; like the reference (which calls csr2ldu on the
+ * caller's arrays directly) the row pointer and columns are used as given. */
+void csr2ldumatrixcreat_(long int* APtrPtr, const double* dataPtr, const int* compRowsPtr,
+                         const int* columnPtr, const int* nCells, const int* size,
+                         const int* symm);
+
+/* fortranInterface.h:44-52 / fortranInterface.cpp:149-197.  Accepted and
+ * ignored on one GPU (single-rank semantics of the reference). */
+void matrixinterfacescreat_(long int* APtrPtr, const int* nNeiProcs, const int* destRank,
+                            const int* locPosition, const int* faceCells, const double* data);
+
+/* fortranInterface.h:55-68 / fortranInterface.cpp:200-268.  Deletes *APtrPtr. */
+void pcgsolversolve_(double* x, long int* APtrPtr, double* b, int* nCells, int* precond,
+                     double* tol, double* relTol, int* maxIter, int* minIter,
+                     int* num_iterations, double* final_res_norm);
+
+/* fortranInterface.h:71-84 / fortranInterface.cpp:271-346.  Deletes *APtrPtr. */
+void pbicgstabsolversolve_(double* x, long int* APtrPtr, double* b, int* nCells, int* precond,
+                           double* tol, double* relTol, int* maxIter, int* minIter,
+                           int* num_iterations, double* final_res_norm);
+
+/* Handle API, fortranInterface.hpp:173-331 / fortranInterface.cpp:537-1102 */
+void contruct_sw_matrix__(long int* APtrPtr, const int* nCellsPtr, const int* rowsPtr,
+                          const int* colsPtr, const int* sizePtr);
+void contruct_sw_matrix_interfaces__(long int* APtrPtr, const int* nNeiProcsPtr,
+                                     const int* destRankPtr, const int* offDiagRowsPtr,
+                                     const int* offDiagStartsPtr);
+void fill_sw_matrix_coefficients__(long int* APtrPtr, const double* diagPtr,
+                                   const double* upperPtr, const double* lowerPtr);
+void fill_sw_matrix_interfaces_coefficients__(long int* APtrPtr, const int* offDiagStartsPtr,
+                                              const double* offDiagCoeffs);
+void contruct_solver_pbicgstab__(long int* solverPtrPtr);
+void sw_solver_pbicgstab_set_maxiter__(long int* solverPtrPtr, const int* maxIterPtr);
+void sw_solver_pbicgstab_set_miniter__(long int* solverPtrPtr, const int* minIterPtr);
+void sw_solver_pbicgstab_set_tol__(long int* solverPtrPtr, const double* tolPtr);
+void sw_solver_pbicgstab_set_reltol__(long int* solverPtrPtr, const double* reltolPtr);
+void sw_solver_pbicgstab_set_precond__(long int* solverPtrPtr, long int* APtrPtr,
+                                       const int* precondTypePtr);
+void sw_solve_pbicgstab__(long int* solverPtrPtr, long int* APtrPtr, double* xPtr,
+                          double* bPtr, double* res_normPtr);
+void sw_matrix_destroy__(long int* APtrPtr);
+void sw_solver_destroy_pbicgstab__(long int* solverPtrPtr);
+
+/* ===================================================================== */
+/* Part 2: GB300 entry points (no counterpart in the reference)          */
+/* ===================================================================== */
+
+typedef struct {
+    int nIterations;
+    int converged;
+    int singular;
+    int status; /* 0 ok */
+    double initialResidual;
+    double finalResidual;
+    double trueResidual; /* ||b - A x|| + 1e-37 when computed, else -1 */
+    double seconds;      /* device time of the solve */
+} unap_cuda_stats;
+
+#define UNAP_CUDA_OK 0
+#define UNAP_CUDA_EINVAL (-1)
+#define UNAP_CUDA_ECUDA (-2)
+#define UNAP_CUDA_ENOMEM (-3)
+#define UNAP_CUDA_EINTERNAL (-4)
+
+/* text of the last error on this thread */
+const char* unap_cuda_last_error(void);
+/* library version string */
+const char* unap_cuda_version(void);
+
+/* Matrix from host LDU arrays (copied).  lower == NULL or lower == upper
+ * makes it symmetric.  *handle receives an opaque handle. */
+int unap_cuda_matrix_create(long int* handle, int nCells, int nFaces, const int* lowerAddr,
+                            const int* upperAddr, const double* lower, const double* diag,
+                            const double* upper);
+int unap_cuda_matrix_destroy(long int handle);
+/* Sizes and host copy of a handle's LDU arrays (any handle from Part 1 or
+ * Part 2; no GPU work).  lower receives upper's values when symmetric. */
+int unap_cuda_matrix_size(long int handle, int* nCells, int* nFaces, int* symm);
+int unap_cuda_matrix_get_ldu(long int handle, int* lowerAddr, int* upperAddr, double* lower,
+                             double* diag, double* upper);
+/* structure facts: forward wavefronts, padded SELL entries, device bytes */
+int unap_cuda_matrix_info(long int handle, int* nWavefronts, long long* nEntries,
+                          long long* deviceBytes);
+
+/* Kernels on device vectors in the caller's cell order (FP64). */
+int unap_cuda_spmv(long int handle, const double* x, double* y);
+/* w = M^-1 r, precond 1 Diag, 2 DIC, 3 DILU */
+int unap_cuda_precondition(long int handle, int precond, const double* r, double* w);
+/* nSweeps Gauss-Seidel sweeps in place on x; backward != 0 sweeps in reverse
+ * cell order (no reference counterpart) */
+int unap_cuda_gauss_seidel(long int handle, double* x, const double* b, int nSweeps,
+                           int backward);
+
+/* PCG (method 0) or PBiCGStab (method 1) with an LDU preconditioner on
+ * device vectors; x holds the initial guess on entry. */
+int unap_cuda_krylov_solve(long int handle, int method, int precond, double tol, double relTol,
+                           int maxIter, int minIter, double* x, const double* b,
+                           unap_cuda_stats* stats);
+
+int unap_cuda_device_synchronize(void);
+
+/* Kernel timings on the matrix's own stream with CUDA events (the GB300
+ * counterpart of the reference's swTimer hooks, src/tools/timers/swTimer.cpp).
+ * Average milliseconds over `reps` after one warm-up, in internal order:
+ * ms[0] SpMV, ms[1] DIC apply (forward + backward sweeps), ms[2] DILU apply,
+ * ms[3] forward Gauss-Seidel sweep, ms[4] backward Gauss-Seidel sweep,
+ * ms[5] FP32 SpMV, ms[6] FP32 forward Gauss-Seidel sweep, ms[7] residual. */
+int unap_cuda_profile_kernels(long int handle, int reps, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* UNAP_CUDA_H */

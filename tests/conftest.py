@@ -1,0 +1,38 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+for p in (ROOT, os.path.join(ROOT, "tests")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def orc():
+    from oracle_lib import Oracle
+    return Oracle("orc")
+
+
+@pytest.fixture(scope="session")
+def ref():
+    from oracle_lib import Oracle, ref_available
+    if not ref_available():
+        pytest.skip("reference build oracle/_ref not present on this host")
+    return Oracle("ref")
+
+
+@pytest.fixture(scope="session")
+def cuda():
+    """torch with a CUDA device, and the product library loaded."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("GPU test on a host without CUDA")
+    from unap_gb300 import capi
+    capi.load()
+    return torch

@@ -1,0 +1,106 @@
+"""Host-side checks of the C ABI that need no GPU: the library loads, exports
+every symbol include/*.h declares, ingests COO/CSR like the reference, and
+reports bad handles as errors instead of crashing."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from unap_gb300 import build, capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if not f.endswith(".h"):
+            continue
+        text = open(os.path.join(inc, f)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([a-z_][a-z0-9_]*)\s*\(",
+                             text, flags=re.M):
+            if m.group(1) not in ("if", "while", "for", "return", "sizeof"):
+                names.append(m.group(1))
+    return sorted(set(names))
+
+
+def test_library_builds_and_loads():
+    path = build.build()
+    assert os.path.exists(path)
+    lib = capi.load()
+    assert b"sm_103a" in lib.unap_cuda_version()
+
+
+def test_every_declared_symbol_is_exported():
+    lib = ctypes.CDLL(build.build())
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # and every declared symbol has a ctypes signature in the Python mirror
+    assert not [n for n in names if n not in capi.SIGNATURES]
+
+
+def test_coo2ldu_known_answer_ex8():
+    # test/ex8.cpp: 5x5 unsymmetric COO (0-based there; the C ABI takes
+    # 1-based indices, fortranInterface.cpp:90-95)
+    row = np.array([0, 0, 0, 0, 1, 1, 1, 2, 2, 2, 3, 3, 3, 4, 4, 4, 4])
+    col = np.array([0, 1, 3, 4, 0, 1, 2, 1, 2, 4, 0, 3, 4, 0, 2, 3, 4])
+    data = np.array([1.1, 1.2, 1.4, 1.5, 2.1, 2.2, 2.3, 3.2, 3.3, 3.5, 4.1, 4.4, 4.5, 5.1, 5.3,
+                     5.4, 5.5])
+    # shuffle columns inside each row: reorderCOO must restore column order
+    perm = np.array([0, 3, 2, 1, 6, 5, 4, 9, 8, 7, 12, 11, 10, 16, 15, 14, 13])
+    h = capi.coo2ldumatrixcreat(data[perm], row[perm] + 1, col[perm] + 1, 5, symm=False)
+    m = capi.handle_ldu(h)
+    capi.sw_matrix_destroy(h)
+    assert list(m["upper_addr"]) == [1, 3, 4, 2, 4, 4]
+    assert list(m["lower_addr"]) == [0, 0, 0, 1, 2, 3]
+    assert np.array_equal(m["diag"], [1.1, 2.2, 3.3, 4.4, 5.5])
+    assert np.array_equal(m["upper"], [1.2, 1.4, 1.5, 2.3, 3.5, 4.5])
+    assert np.array_equal(m["lower"], [2.1, 4.1, 5.1, 3.2, 5.3, 5.4])
+    assert not m["symm"]
+
+
+def test_coo2ldu_against_reference(ref):
+    # random structurally symmetric COO, row-sorted, columns shuffled per row
+    rng = np.random.default_rng(5)
+    from unap_gb300 import workloads as W
+    s = W.convdiff(4, 3, 3, seed=2, permute=True)
+    a = s.dense()
+    r, c = np.nonzero(a)
+    v = a[r, c]
+    h = capi.coo2ldumatrixcreat(v, r + 1, c + 1, s.n, symm=False)
+    m = capi.handle_ldu(h)
+    capi.sw_matrix_destroy(h)
+    vp = ctypes.c_void_p
+    r32 = r.astype(np.int32)
+    c32 = c.astype(np.int32)
+    Aref = ref.lib.ref_coo2ldu(vp(v.ctypes.data), vp(r32.ctypes.data), vp(c32.ctypes.data),
+                               s.n, len(v), 0)
+    nf = ref.lib.ref_ldu_nfaces(ctypes.c_void_p(Aref))
+    l = np.zeros(nf, np.int32)
+    u = np.zeros(nf, np.int32)
+    lo = np.zeros(nf)
+    d = np.zeros(s.n)
+    up = np.zeros(nf)
+    ref.lib.ref_ldu_get(vp(Aref), vp(l.ctypes.data), vp(u.ctypes.data), vp(lo.ctypes.data),
+                        vp(d.ctypes.data), vp(up.ctypes.data))
+    ref.lib.ref_ldu_destroy(ctypes.c_void_p(Aref))
+    for k, v2 in (("lower_addr", l), ("upper_addr", u), ("lower", lo), ("diag", d),
+                  ("upper", up)):
+        assert np.array_equal(m[k], v2), k
+    del rng
+
+
+def test_bad_handle_is_an_error_not_a_crash():
+    lib = capi.load()
+    bogus = np.zeros(8, np.int64)  # valid memory without the handle magic
+    rc = lib.unap_cuda_matrix_destroy(bogus.ctypes.data)
+    assert rc == -1
+    assert b"invalid matrix handle" in lib.unap_cuda_last_error()
+    with pytest.raises(capi.UnapCudaError):
+        capi.handle_ldu(bogus.ctypes.data)

@@ -1,0 +1,138 @@
+"""GPU parity of the CUDA path against the oracle, through the C ABI.
+
+Kernels that keep the reference's per-row operation order (SpMV, Diag/DIC/
+DILU factor and sweeps, Gauss-Seidel) must be bit-identical to the oracle.
+Krylov solves differ only in the summation order of dot products: the
+iteration count must match within +-1 and the solution within 1e-10 relative
+2-norm (the parity bar for floating-point results on this path).
+"""
+import numpy as np
+import pytest
+
+import golden_cases
+from unap_gb300 import capi
+from unap_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+SOL_RTOL = 1e-10
+
+
+def systems():
+    out = [s for s, _ in golden_cases.load()]
+    out += [W.laplace(16, 12, 10, seed=1, permute=True, rhs="normal"),
+            W.laplace(12, seed=2, permute=False),
+            W.convdiff(14, 12, 10, seed=3, permute=True, pe=5.0),
+            W.lognormal(16, seed=4, permute=True)]
+    return out
+
+
+def ring10():
+    # test/ex2.cpp ring: the last face (0, 9) breaks owner order
+    n = 10
+    lo = np.array([i if i < n - 1 else 0 for i in range(n)], np.int32)
+    up = np.array([i + 1 if i < n - 1 else n - 1 for i in range(n)], np.int32)
+    return W.LduSystem(n, lo, up, np.full(n, -1.0), np.full(n, 4.0), np.full(n, -1.0),
+                       np.zeros(n))
+
+
+def dev(torch, a):
+    return torch.tensor(np.asarray(a, dtype=np.float64), device="cuda")
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+def test_spmv_bit_exact(cuda, orc):
+    torch = cuda
+    for s in systems() + [ring10()]:
+        A = capi.DeviceMatrix(s)
+        x = np.random.default_rng(s.n).standard_normal(s.n)
+        y = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+        A.spmv(dev(torch, x), y)
+        assert np.array_equal(host(y), orc.spmv(s, x)), s.name
+        A.close()
+
+
+def test_ex2_known_answer_on_gpu(cuda):
+    torch = cuda
+    s = ring10()
+    A = capi.DeviceMatrix(s)
+    y = torch.zeros(10, dtype=torch.float64, device="cuda")
+    A.spmv(dev(torch, (np.arange(10) + 0.2) / 0.4), y)
+    assert np.allclose(host(y), [-24, 6, 11, 16, 21, 26, 31, 36, 41, 71], rtol=0, atol=1e-12)
+
+
+def test_preconditioners_bit_exact(cuda, orc):
+    torch = cuda
+    for s in systems():
+        A = capi.DeviceMatrix(s)
+        r = np.random.default_rng(s.n + 1).standard_normal(s.n)
+        for t in (1, 2, 3):
+            w = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+            A.precondition(t, dev(torch, r), w)
+            w_ref, _ = orc.precond(t, s, r)
+            assert np.array_equal(host(w), w_ref), (s.name, t)
+        A.close()
+
+
+def test_gauss_seidel_bit_exact(cuda, orc):
+    torch = cuda
+    for s in systems():
+        A = capi.DeviceMatrix(s)
+        x0 = np.random.default_rng(s.n + 2).standard_normal(s.n)
+        for backward in (False, True):
+            x = dev(torch, x0)
+            A.gauss_seidel(x, dev(torch, s.b), 3, backward=backward)
+            assert np.array_equal(host(x), orc.gs(s, x0, s.b, 3, backward=backward)), (
+                s.name, backward)
+        A.close()
+
+
+def _solution_close(x, x_ref):
+    return np.linalg.norm(x - x_ref) <= SOL_RTOL * max(np.linalg.norm(x_ref), 1e-300)
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_krylov_parity(cuda, orc, method):
+    torch = cuda
+    for s in systems():
+        A = capi.DeviceMatrix(s)
+        for t in (0, 1, 2, 3):
+            if method == 0 and not s.symm and t == 2:
+                continue
+            x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+            st = A.krylov_solve(method, t, x, dev(torch, s.b), rel_tol=1e-8, max_iter=500)
+            if method == 0:
+                x_ref, st_ref = orc.pcg(s, t, s.b, rel_tol=1e-8, max_iter=500)
+            else:
+                x_ref, st_ref = orc.pbicgstab(s, t, s.b, rel_tol=1e-8, max_iter=500)
+            assert abs(st["nIterations"] - st_ref["n_iter"]) <= 1, (s.name, method, t, st, st_ref)
+            assert st["converged"] == st_ref["converged"]
+            assert np.isclose(st["initialResidual"], st_ref["init_res"], rtol=1e-12)
+            assert _solution_close(host(x), x_ref), (s.name, method, t)
+        A.close()
+
+
+def test_fortran_oneshot_ex3(cuda):
+    # test/ex3.cpp through pcgsolversolve_: x = (2, -2) after 1 iteration
+    s = W.LduSystem(2, np.array([0], np.int32), np.array([1], np.int32), None,
+                    np.array([3.0, 6.0]), np.array([2.0]), np.array([2.0, -8.0]))
+    h = capi.ldumatrixcreat(s)
+    x, it, res = capi.pcgsolversolve(np.zeros(2), h, s.b, precond=2)
+    assert it == 1
+    assert np.allclose(x, [2.0, -2.0], atol=1e-14)
+
+
+def test_fortran_oneshot_matches_oracle(cuda, orc):
+    for s in systems()[:4]:
+        for fn, ofn, t in ((capi.pcgsolversolve, orc.pcg, 2),
+                           (capi.pbicgstabsolversolve, orc.pbicgstab, 3)):
+            if fn is capi.pcgsolversolve and not s.symm:
+                continue
+            h = capi.ldumatrixcreat(s)
+            x, it, res = fn(np.zeros(s.n), h, s.b, precond=t, rel_tol=1e-9)
+            x_ref, st = ofn(s, t, s.b, rel_tol=1e-9)
+            assert abs(it - st["n_iter"]) <= 1
+            assert _solution_close(x, x_ref)

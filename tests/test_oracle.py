@@ -1,0 +1,151 @@
+"""The C restatement (oracle/unap_oracle.c) against the reference.
+
+* against tests/golden/reference_small.npz (outputs of the reference library
+  on seeded systems; runs on every host);
+* against the reference's own known answers (test/ex2.cpp, test/ex3.cpp);
+* against the reference library itself on freshly generated systems, where
+  oracle/_ref was built on this host.
+
+Every comparison is bit-exact: both codes run the same loops with the same
+operation order and no fused multiply-adds.
+"""
+import numpy as np
+import pytest
+
+import golden_cases
+from unap_gb300 import workloads as W
+
+
+def _eq(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return a.shape == b.shape and np.array_equal(a, b)
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return golden_cases.load()
+
+
+def test_golden_kernels(orc, golden):
+    for s, g in golden:
+        x = g["x"]
+        assert _eq(orc.spmv(s, x), g["spmv"]), s.name
+        for t in (1, 2, 3):
+            w, rD = orc.precond(t, s, x)
+            assert _eq(w, g[f"precond{t}_w"]) and _eq(rD, g[f"precond{t}_rD"]), (s.name, t)
+        assert _eq(orc.gs(s, x, s.b, 3), g["gs3"]), s.name
+        assert _eq(orc.cheby(s, x, s.b, 3, 3), g["cheby3x3"]), s.name
+        e, xe = orc.eigen(s, x, s.b)
+        assert e == float(g["eig"]) and _eq(xe, g["eig_x"]), s.name
+
+
+def test_golden_krylov(orc, golden):
+    for s, g in golden:
+        for t in (0, 1, 2, 3):
+            x, st = orc.pcg(s, t, s.b, rel_tol=1e-8)
+            ref = g[f"pcg{t}_stats"]
+            assert _eq(x, g[f"pcg{t}_x"]), (s.name, "pcg", t)
+            assert st["n_iter"] == int(ref[0]) and st["final_res"] == ref[2]
+            x, st = orc.pbicgstab(s, t, s.b, rel_tol=1e-8)
+            ref = g[f"bicg{t}_stats"]
+            assert _eq(x, g[f"bicg{t}_x"]), (s.name, "bicg", t)
+            assert st["n_iter"] == int(ref[0]) and st["final_res"] == ref[2]
+
+
+def test_golden_hierarchy_and_mg(orc, golden):
+    for s, g in golden:
+        w = np.abs(s.upper) / np.sqrt(np.sum(s.upper ** 2))
+        levels = orc.hierarchy(s, w, n_coarsest=8)
+        assert len(levels) == int(g["nlevels"]), s.name
+        for li, L in enumerate(levels):
+            for key in ("restrict", "face_restrict", "lower_addr", "upper_addr", "diag", "upper",
+                        "lower"):
+                if key == "lower" and s.symm:
+                    continue
+                assert _eq(L[key], g[f"L{li}_{key}"]), (s.name, li, key)
+        for sm in (1, 2):
+            x, st = orc.mg(s, s.b, w, n_coarsest=8, smoother=sm, rel_tol=1e-8, max_iter=60)
+            ref = g[f"mg{sm}_stats"]
+            assert _eq(x, g[f"mg{sm}_x"]), (s.name, sm)
+            assert st["n_iter"] == int(ref[0]) and st["n_levels"] == int(ref[4])
+
+
+def test_known_answer_ex2_spmv(orc):
+    # test/ex2.cpp: 10-cell ring, diag 4, off-diagonals -1, x = (i + 0.2)/0.4;
+    # the reference prints Apsi = (-24, 6, 11, 16, 21, 26, 31, 36, 41, 71)
+    n = 10
+    lo_addr = np.array([i if i < n - 1 else 0 for i in range(n)], np.int32)
+    up_addr = np.array([i + 1 if i < n - 1 else n - 1 for i in range(n)], np.int32)
+    s = W.LduSystem(n, lo_addr, up_addr, np.full(n, -1.0), np.full(n, 4.0), np.full(n, -1.0),
+                    np.zeros(n))
+    y = orc.spmv(s, (np.arange(n) + 0.2) / 0.4)
+    assert np.allclose(y, [-24, 6, 11, 16, 21, 26, 31, 36, 41, 71], rtol=0, atol=1e-12)
+
+
+def test_known_answer_ex3_pcg(orc):
+    # test/ex3.cpp: A = [[3,2],[2,6]], b = (2,-8), PCG+DIC -> x = (2,-2) in 1 iteration
+    s = W.LduSystem(2, np.array([0], np.int32), np.array([1], np.int32), np.array([2.0]),
+                    np.array([3.0, 6.0]), np.array([2.0]), np.array([2.0, -8.0]))
+    x, st = orc.pcg(s, 2, s.b)
+    assert st["n_iter"] == 1
+    assert np.allclose(x, [2.0, -2.0], atol=1e-14)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_against_reference_library(orc, ref, seed):
+    cases = [W.laplace(5, 6, 4, seed=seed, permute=True, rhs="normal"),
+             W.convdiff(5, 5, 5, seed=seed, permute=True, pe=3.0 + seed),
+             W.lognormal(7, 6, 5, seed=seed, permute=True)]
+    for s in cases:
+        x = np.random.default_rng(seed).standard_normal(s.n)
+        assert _eq(orc.spmv(s, x), ref.spmv(s, x))
+        for a, b in zip(orc.losort(s), ref.losort(s)):
+            assert _eq(a, b)
+        for t in (1, 2, 3):
+            assert all(_eq(a, b) for a, b in zip(orc.precond(t, s, x), ref.precond(t, s, x)))
+        assert _eq(orc.gs(s, x, s.b, 2), ref.gs(s, x, s.b, 2))
+        assert _eq(orc.cheby(s, x, s.b, 4, 2), ref.cheby(s, x, s.b, 4, 2))
+        for t in (0, 2, 3):
+            a, b = orc.pcg(s, t, s.b, rel_tol=1e-9), ref.pcg(s, t, s.b, rel_tol=1e-9)
+            assert _eq(a[0], b[0]) and a[1] == b[1]
+            a, b = orc.pbicgstab(s, t, s.b, rel_tol=1e-9), ref.pbicgstab(s, t, s.b, rel_tol=1e-9)
+            assert _eq(a[0], b[0]) and a[1] == b[1]
+        w = np.abs(s.upper) / np.sqrt(np.sum(s.upper ** 2))
+        h1, h2 = orc.hierarchy(s, w, n_coarsest=6), ref.hierarchy(s, w, n_coarsest=6)
+        assert len(h1) == len(h2)
+        for L1, L2 in zip(h1, h2):
+            for k in ("restrict", "face_restrict", "lower_addr", "upper_addr", "diag", "upper"):
+                assert _eq(L1[k], L2[k]), k
+        for sm in (1, 2):
+            a = orc.mg(s, s.b, w, n_coarsest=6, smoother=sm, rel_tol=1e-8, max_iter=40)
+            b = ref.mg(s, s.b, w, n_coarsest=6, smoother=sm, rel_tol=1e-8, max_iter=40)
+            assert _eq(a[0], b[0]) and a[1] == b[1]
+
+
+def test_mg_options_against_reference(orc, ref):
+    # pre-smoothing, no correction scaling, maxLevels limit
+    s = W.laplace(6, 6, 5, seed=7, permute=True, rhs="normal")
+    w = np.abs(s.upper) / np.sqrt(np.sum(s.upper ** 2))
+    for kw in (dict(n_pre=2), dict(scale_corr=0), dict(max_levels=3, n_post=1, n_finest=3)):
+        for sm in (1, 2):
+            a = orc.mg(s, s.b, w, n_coarsest=5, smoother=sm, rel_tol=1e-8, max_iter=30, **kw)
+            b = ref.mg(s, s.b, w, n_coarsest=5, smoother=sm, rel_tol=1e-8, max_iter=30, **kw)
+            assert _eq(a[0], b[0]) and a[1] == b[1], kw
+
+
+def test_amg_pcg_oracle_converges(orc):
+    # NEW component (no reference counterpart): AMG-PCG with SGS, dense coarsest
+    from oracle_lib import OracleAmg
+    s = W.lognormal(12, seed=3)
+    for prec in (0, 1):
+        A = OracleAmg(orc, s, n_coarsest=60, precision=prec, flexible=prec, rel_tol=1e-10)
+        sizes = A.level_sizes()
+        assert sizes[-1] <= 60 and sizes[0] == s.n
+        x, st = A.solve(s.b)
+        assert st["converged"]
+        r = s.b - orc.spmv(s, x)
+        assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(s.b)
+        inv = A.coarse_inverse()
+        assert np.allclose(inv, inv.T, rtol=0, atol=0)
+        A.close()

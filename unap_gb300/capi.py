@@ -1,0 +1,284 @@
+"""ctypes binding of libunap_cuda.so (include/unap_cuda.h).
+
+This is the Python-side mirror of UNAP's foreign interface: the reference's
+Fortran-convention calls (``ldumatrixcreat_``, ``pcgsolversolve_`` ...) are
+exposed under the same names with the same argument meaning, and the GB300
+``unap_cuda_*`` entry points are wrapped for device-resident vectors (any
+object with a ``data_ptr()`` such as a CUDA torch tensor, or a raw int).
+
+The library must be built (``unap_gb300.build.build()``); importing a missing
+library raises instead of falling back to anything.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_c_int = ctypes.c_int
+_c_long = ctypes.c_long
+_c_ll = ctypes.c_longlong
+_c_dbl = ctypes.c_double
+_vp = ctypes.c_void_p
+_ip = ctypes.POINTER(ctypes.c_int)
+_dp = ctypes.POINTER(ctypes.c_double)
+_lp = ctypes.POINTER(ctypes.c_long)
+
+_LIB = None
+
+
+class UnapCudaError(RuntimeError):
+    pass
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("nIterations", _c_int), ("converged", _c_int), ("singular", _c_int),
+                ("status", _c_int), ("initialResidual", _c_dbl), ("finalResidual", _c_dbl),
+                ("trueResidual", _c_dbl), ("seconds", _c_dbl)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# name -> (restype, argtypes); the exported C symbols of include/unap_cuda.h
+SIGNATURES = {
+    "ldumatrixcreat_": (None, [_lp, _ip, _ip, _ip, _ip, _dp, _dp, _dp]),
+    "coo2ldumatrixcreat_": (None, [_lp, _dp, _ip, _ip, _ip, _ip, _ip]),
+    "csr2ldumatrixcreat_": (None, [_lp, _dp, _ip, _ip, _ip, _ip, _ip]),
+    "matrixinterfacescreat_": (None, [_lp, _ip, _ip, _ip, _ip, _dp]),
+    "pcgsolversolve_": (None, [_dp, _lp, _dp, _ip, _ip, _dp, _dp, _ip, _ip, _ip, _dp]),
+    "pbicgstabsolversolve_": (None, [_dp, _lp, _dp, _ip, _ip, _dp, _dp, _ip, _ip, _ip, _dp]),
+    "contruct_sw_matrix__": (None, [_lp, _ip, _ip, _ip, _ip]),
+    "contruct_sw_matrix_interfaces__": (None, [_lp, _ip, _ip, _ip, _ip]),
+    "fill_sw_matrix_coefficients__": (None, [_lp, _dp, _dp, _dp]),
+    "fill_sw_matrix_interfaces_coefficients__": (None, [_lp, _ip, _dp]),
+    "contruct_solver_pbicgstab__": (None, [_lp]),
+    "sw_solver_pbicgstab_set_maxiter__": (None, [_lp, _ip]),
+    "sw_solver_pbicgstab_set_miniter__": (None, [_lp, _ip]),
+    "sw_solver_pbicgstab_set_tol__": (None, [_lp, _dp]),
+    "sw_solver_pbicgstab_set_reltol__": (None, [_lp, _dp]),
+    "sw_solver_pbicgstab_set_precond__": (None, [_lp, _lp, _ip]),
+    "sw_solve_pbicgstab__": (None, [_lp, _lp, _dp, _dp, _dp]),
+    "sw_matrix_destroy__": (None, [_lp]),
+    "sw_solver_destroy_pbicgstab__": (None, [_lp]),
+    "unap_cuda_last_error": (ctypes.c_char_p, []),
+    "unap_cuda_version": (ctypes.c_char_p, []),
+    "unap_cuda_device_synchronize": (_c_int, []),
+    "unap_cuda_matrix_create": (_c_int, [_lp, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp]),
+    "unap_cuda_matrix_destroy": (_c_int, [_c_long]),
+    "unap_cuda_matrix_size": (_c_int, [_c_long, _ip, _ip, _ip]),
+    "unap_cuda_matrix_get_ldu": (_c_int, [_c_long, _vp, _vp, _vp, _vp, _vp]),
+    "unap_cuda_matrix_info": (_c_int, [_c_long, _ip, ctypes.POINTER(_c_ll),
+                                       ctypes.POINTER(_c_ll)]),
+    "unap_cuda_spmv": (_c_int, [_c_long, _vp, _vp]),
+    "unap_cuda_profile_kernels": (_c_int, [_c_long, _c_int, _vp]),
+    "unap_cuda_precondition": (_c_int, [_c_long, _c_int, _vp, _vp]),
+    "unap_cuda_gauss_seidel": (_c_int, [_c_long, _vp, _vp, _c_int, _c_int]),
+    "unap_cuda_krylov_solve": (_c_int, [_c_long, _c_int, _c_int, _c_dbl, _c_dbl, _c_int,
+                                        _c_int, _vp, _vp, ctypes.POINTER(Stats)]),
+}
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libunap_cuda.so (building it first if it is missing)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise UnapCudaError(f"{path} is not built")
+        _build.build()
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        msg = load().unap_cuda_last_error().decode(errors="replace")
+        raise UnapCudaError(f"unap_cuda error {rc}: {msg}")
+
+
+def _ptr(t) -> int | None:
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data
+    return t.data_ptr()
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _as_ip(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _as_dp(a):
+    return a.ctypes.data_as(_dp)
+
+
+class DeviceMatrix:
+    """An LDU matrix resident on the GPU (``unap_cuda_matrix_create``)."""
+
+    def __init__(self, system):
+        lib = load()
+        self._keep = (_i32(system.lower_addr), _i32(system.upper_addr),
+                      None if system.symm else _f64(system.lower), _f64(system.diag),
+                      _f64(system.upper))
+        l, u, lo, d, up = self._keep
+        h = _c_long(0)
+        check(lib.unap_cuda_matrix_create(ctypes.byref(h), system.n, system.nf, l.ctypes.data,
+                                          u.ctypes.data, None if lo is None else lo.ctypes.data,
+                                          d.ctypes.data, up.ctypes.data))
+        self.handle = h.value
+        self.n = system.n
+        self._keep = None
+
+    def info(self):
+        w = _c_int()
+        e = _c_ll()
+        b = _c_ll()
+        check(load().unap_cuda_matrix_info(self.handle, ctypes.byref(w), ctypes.byref(e),
+                                           ctypes.byref(b)))
+        return dict(n_wavefronts=w.value, n_entries=e.value, device_bytes=b.value)
+
+    def spmv(self, x, y):
+        check(load().unap_cuda_spmv(self.handle, _ptr(x), _ptr(y)))
+
+    def precondition(self, ptype, r, w):
+        check(load().unap_cuda_precondition(self.handle, ptype, _ptr(r), _ptr(w)))
+
+    def gauss_seidel(self, x, b, n_sweeps, backward=False):
+        check(load().unap_cuda_gauss_seidel(self.handle, _ptr(x), _ptr(b), n_sweeps,
+                                            1 if backward else 0))
+
+    def krylov_solve(self, method, precond, x, b, tol=0.0, rel_tol=1e-6, max_iter=1000,
+                     min_iter=0):
+        st = Stats()
+        check(load().unap_cuda_krylov_solve(self.handle, method, precond, tol, rel_tol,
+                                            max_iter, min_iter, _ptr(x), _ptr(b),
+                                            ctypes.byref(st)))
+        return st.as_dict()
+
+    def profile(self, reps=20):
+        ms = np.zeros(8)
+        check(load().unap_cuda_profile_kernels(self.handle, reps, ms.ctypes.data))
+        keys = ["spmv", "dic_apply", "dilu_apply", "gs_fwd", "gs_bwd", "spmv32", "gs_fwd32",
+                "residual"]
+        return dict(zip(keys, ms.tolist()))
+
+    def close(self):
+        if self.handle:
+            check(load().unap_cuda_matrix_destroy(self.handle))
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---- the reference's Fortran-convention calls, host arrays ----------------
+
+def ldumatrixcreat(system) -> int:
+    """ldumatrixcreat_ (fortranInterface.cpp:31-71); returns the handle."""
+    lib = load()
+    h = _c_long(0)
+    n = _c_int(system.n)
+    nf = _c_int(system.nf)
+    l = _i32(system.lower_addr)
+    u = _i32(system.upper_addr)
+    up = _f64(system.upper)
+    lo = up if system.symm else _f64(system.lower)
+    d = _f64(system.diag)
+    lib.ldumatrixcreat_(ctypes.byref(h), ctypes.byref(n), ctypes.byref(nf), _as_ip(l), _as_ip(u),
+                        _as_dp(lo), _as_dp(d), _as_dp(up))
+    if not h.value:
+        raise UnapCudaError(load().unap_cuda_last_error().decode())
+    return h.value
+
+
+def _krylov_oneshot(fn_name, x, handle, b, precond, tol, rel_tol, max_iter, min_iter):
+    lib = load()
+    x = _f64(x)
+    b = _f64(b)
+    h = _c_long(handle)
+    n = _c_int(x.shape[0])
+    it = _c_int(0)
+    res = _c_dbl(0)
+    getattr(lib, fn_name)(_as_dp(x), ctypes.byref(h), _as_dp(b), ctypes.byref(n),
+                          ctypes.byref(_c_int(precond)), ctypes.byref(_c_dbl(tol)),
+                          ctypes.byref(_c_dbl(rel_tol)), ctypes.byref(_c_int(max_iter)),
+                          ctypes.byref(_c_int(min_iter)), ctypes.byref(it), ctypes.byref(res))
+    return x, it.value, res.value
+
+
+def pcgsolversolve(x, handle, b, precond, tol=0.0, rel_tol=1e-6, max_iter=1000, min_iter=0):
+    """pcgsolversolve_ (fortranInterface.cpp:200-268).  Consumes the handle."""
+    return _krylov_oneshot("pcgsolversolve_", x, handle, b, precond, tol, rel_tol, max_iter,
+                           min_iter)
+
+
+def pbicgstabsolversolve(x, handle, b, precond, tol=0.0, rel_tol=1e-6, max_iter=1000,
+                         min_iter=0):
+    """pbicgstabsolversolve_ (fortranInterface.cpp:271-346).  Consumes the handle."""
+    return _krylov_oneshot("pbicgstabsolversolve_", x, handle, b, precond, tol, rel_tol,
+                           max_iter, min_iter)
+
+
+def handle_ldu(handle: int) -> dict:
+    """Host copy of a matrix handle's LDU arrays (no GPU work)."""
+    lib = load()
+    n = _c_int()
+    nf = _c_int()
+    sy = _c_int()
+    check(lib.unap_cuda_matrix_size(handle, ctypes.byref(n), ctypes.byref(nf), ctypes.byref(sy)))
+    l = np.zeros(nf.value, np.int32)
+    u = np.zeros(nf.value, np.int32)
+    lo = np.zeros(nf.value)
+    up = np.zeros(nf.value)
+    d = np.zeros(n.value)
+    check(lib.unap_cuda_matrix_get_ldu(handle, l.ctypes.data, u.ctypes.data, lo.ctypes.data,
+                                       d.ctypes.data, up.ctypes.data))
+    return dict(n=n.value, nf=nf.value, symm=bool(sy.value), lower_addr=l, upper_addr=u,
+                lower=lo, diag=d, upper=up)
+
+
+def coo2ldumatrixcreat(data, rows_1based, cols_1based, n_cells, symm) -> int:
+    """coo2ldumatrixcreat_ (fortranInterface.cpp:74-120); returns the handle."""
+    lib = load()
+    h = _c_long(0)
+    d = _f64(data)
+    r = _i32(rows_1based)
+    c = _i32(cols_1based)
+    lib.coo2ldumatrixcreat_(ctypes.byref(h), _as_dp(d), _as_ip(r), _as_ip(c),
+                            ctypes.byref(_c_int(n_cells)), ctypes.byref(_c_int(d.shape[0])),
+                            ctypes.byref(_c_int(1 if symm else 0)))
+    if not h.value:
+        raise UnapCudaError(lib.unap_cuda_last_error().decode())
+    return h.value
+
+
+def sw_matrix_destroy(handle: int) -> None:
+    load().sw_matrix_destroy__(ctypes.byref(_c_long(handle)))

@@ -1,0 +1,363 @@
+// Host-side engine: matrices, LDU preconditioners and the PCG / PBiCGStab
+// drivers.  One solve keeps every vector and scalar on the device; the host
+// only enqueues gated iterations (captured once into a CUDA graph) and polls
+// the `done` flag of the device solver state between batches.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "engine.hpp"
+
+namespace unapgpu {
+
+// ---- error text ---------------------------------------------------------
+static thread_local std::string g_last_error;
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+const char* last_error() { return g_last_error.c_str(); }
+
+// ---- Matrix ----------------------------------------------------------------
+Matrix::Matrix(HostLdu&& h, cudaStream_t s) : host(std::move(h)), stream(s)
+{
+    if (!stream) {
+        UNAP_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        ownsStream = true;
+    }
+    host.validate();
+    L = build_level(host, nullptr, false, stream);
+}
+
+Matrix::~Matrix()
+{
+    L.reset();
+    if (ownsStream && stream) cudaStreamDestroy(stream);
+}
+
+void Matrix::setValues(const double* diag, const double* upper, const double* lower)
+{
+    std::memcpy(host.diag.data(), diag, sizeof(double) * (size_t)host.n);
+    std::memcpy(host.upper.data(), upper, sizeof(double) * (size_t)host.nf);
+    bool symm = (lower == nullptr || lower == upper);
+    host.symm = symm;
+    if (symm)
+        host.lower.clear();
+    else
+        host.lower.assign(lower, lower + host.nf);
+    update_level_values(*L, host, stream);
+}
+
+// ---- preconditioners -------------------------------------------------------
+namespace {
+
+class NoPrecond : public Precond {
+public:
+    explicit NoPrecond(int n) : n(n) {}
+    bool fusesDot() const override { return true; }
+    void apply(const Exec& ex, const double* r, double* w, const RedPool* pool, int site,
+               KState* st, int fin, Gate g) override
+    {
+        // identity preconditioner (unapMatrixPrecond.cpp:4-17)
+        diag_apply(ex, n, nullptr, r, w, pool ? pool->site(site, st, fin) : RSpec{}, g);
+    }
+    int n;
+};
+
+class DiagPrecond : public Precond {
+public:
+    explicit DiagPrecond(Matrix& A) : n(A.n())
+    {
+        // lduDiagPrecond.cpp:13-41: rD = 1 / D
+        std::vector<double> h((size_t)n);
+        for (int i = 0; i < n; ++i) h[(size_t)i] = 1.0 / A.host.diag[(size_t)A.L->perm[(size_t)i]];
+        rD.upload(h, A.stream);
+        UNAP_CK(cudaStreamSynchronize(A.stream));
+    }
+    bool fusesDot() const override { return true; }
+    void apply(const Exec& ex, const double* r, double* w, const RedPool* pool, int site,
+               KState* st, int fin, Gate g) override
+    {
+        diag_apply(ex, n, rD.p, r, w, pool ? pool->site(site, st, fin) : RSpec{}, g);
+    }
+    int n;
+    DevArray<double> rD;
+};
+
+class DicPrecond : public Precond {
+public:
+    DicPrecond(Matrix& A, bool dilu) : L(*A.L), dilu(dilu)
+    {
+        if (!L.sweepable)
+            throw std::invalid_argument(
+                "DIC/DILU need faces oriented lowerAddr < upperAddr and sorted by owner");
+        Exec ex;
+        ex.s = A.stream;
+        ex.maxBlocks = device_max_blocks();
+        dfac.alloc((size_t)L.n);
+        rD.alloc((size_t)L.n);
+        dic_factor(ex, L, dilu, dfac.p, rD.p);
+        UNAP_CK(cudaGetLastError());
+        UNAP_CK(cudaStreamSynchronize(A.stream));
+    }
+    bool fusesDot() const override { return true; }
+    void apply(const Exec& ex, const double* r, double* w, const RedPool* pool, int site,
+               KState* st, int fin, Gate g) override
+    {
+        dic_apply(ex, L, dilu, rD.p, r, w, pool, site, st, fin, g);
+    }
+    const Level& L;
+    bool dilu;
+    DevArray<double> dfac, rD;
+};
+
+}  // namespace
+
+std::unique_ptr<Precond> make_ldu_precond(int type, Matrix& A)
+{
+    // fortranInterface.cpp:227-238: 1 Diag, 2 DIC, 3 DILU, otherwise none
+    if (type == 1) return std::make_unique<DiagPrecond>(A);
+    if (type == 2) return std::make_unique<DicPrecond>(A, false);
+    if (type == 3) return std::make_unique<DicPrecond>(A, true);
+    return std::make_unique<NoPrecond>(A.n());
+}
+
+// ---- Krylov driver -------------------------------------------------------------
+enum { S_INIT = 0, S_WR, S_ALPHA, S_RES, S_TRUE, S_BS, S_BOMEGA, S_NSITES };
+
+Krylov::Krylov(Matrix& A_, Precond* P_, Method m) : A(A_), P(P_), method(m)
+{
+    n = A.n();
+    ex.s = A.stream;
+    ex.maxBlocks = device_max_blocks();
+    size_t N = (size_t)n;
+    x.alloc(N);
+    b.alloc(N);
+    r.alloc(N);
+    z.alloc(N);
+    p.alloc(N);
+    q.alloc(N);
+    if (method == Method::PBiCGStab) {
+        r0.alloc(N);
+        y.alloc(N);
+        Ay.alloc(N);
+        s.alloc(N);
+        t.alloc(N);
+    }
+    UNAP_CK(cudaMalloc((void**)&d_st, sizeof(KState)));
+    UNAP_CK(cudaMallocHost((void**)&h_st, sizeof(KState)));
+    pool.init(S_NSITES, ex.maxBlocks, std::max(1, A.L->nWave) + 1, ex.s);
+    UNAP_CK(cudaEventCreate(&ev0));
+    UNAP_CK(cudaEventCreate(&ev1));
+}
+
+Krylov::~Krylov()
+{
+    if (graphExec) cudaGraphExecDestroy(graphExec);
+    if (graph) cudaGraphDestroy(graph);
+    if (d_st) cudaFree(d_st);
+    if (h_st) cudaFreeHost(h_st);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+}
+
+void Krylov::initState()
+{
+    KState h;
+    std::memset(&h, 0, sizeof(h));
+    h.wArA = 1.0e37;  // GREAT, PCG.cpp:57
+    h.tol = tol;
+    h.relTol = relTol;
+    h.maxIter = maxIter;
+    h.minIter = minIter;
+    h.first = 1;
+    h.flexible = flexible ? 1 : 0;
+    h.trueRes = -1.0;
+    *h_st = h;
+    UNAP_CK(cudaMemcpyAsync(d_st, h_st, sizeof(KState), cudaMemcpyHostToDevice, ex.s));
+}
+
+void Krylov::readState()
+{
+    UNAP_CK(cudaMemcpyAsync(h_st, d_st, sizeof(KState), cudaMemcpyDeviceToHost, ex.s));
+    UNAP_CK(cudaStreamSynchronize(ex.s));
+}
+
+// PCG.cpp:97-180 with the vector work fused into four kernels (plus the
+// preconditioner's own sweeps).  wA of the reference is split into z
+// (preconditioned residual) and q (A p) so flexible PCG can use z.q.
+void Krylov::enqueuePcgIteration()
+{
+    Gate g{d_st, 1};
+    Rows<double> Ar = rows64(*A.L);
+    if (P->fusesDot() && !flexible) {
+        P->apply(ex, r.p, z.p, &pool, S_WR, d_st, FIN_PCG_WR, g);
+    } else {
+        P->apply(ex, r.p, z.p, nullptr, 0, d_st, FIN_NONE, g);
+        k_dot2(ex, n, z.p, r.p, flexible ? z.p : nullptr, flexible ? q.p : nullptr,
+               pool.site(S_WR, d_st, FIN_PCG_WR), g);
+    }
+    k_pcg_direction(ex, n, z.p, p.p, d_st, g);
+    k_spmv<double>(ex, Ar, p.p, q.p, p.p, pool.site(S_ALPHA, d_st, FIN_PCG_ALPHA), g);
+    k_pcg_update(ex, n, x.p, r.p, p.p, q.p, pool.site(S_RES, d_st, FIN_PCG_RES), g);
+}
+
+// PBiCGStab.cpp:155-456.  rA0.rA of the next iteration is fused into the
+// update kernel; `early` (converged on ||s||) gates the second half.
+void Krylov::enqueueBicgIteration()
+{
+    Gate g3{d_st, 3}, g1{d_st, 1};
+    Rows<double> Ar = rows64(*A.L);
+    k_bicg_direction(ex, n, r.p, Ay.p, p.p, d_st, g3);
+    P->apply(ex, p.p, y.p, nullptr, 0, d_st, FIN_NONE, g3);
+    k_spmv<double>(ex, Ar, y.p, Ay.p, r0.p, pool.site(S_ALPHA, d_st, FIN_BICG_ALPHA), g3);
+    k_bicg_s(ex, n, r.p, Ay.p, s.p, pool.site(S_BS, d_st, FIN_BICG_S), g3);
+    P->apply(ex, s.p, z.p, nullptr, 0, d_st, FIN_NONE, g3);
+    // t = A z; tAtA = t.t and omega numerator t.s
+    k_spmv<double>(ex, Ar, z.p, t.p, nullptr, RSpec{}, g3);
+    k_dot2(ex, n, t.p, t.p, t.p, s.p, pool.site(S_BOMEGA, d_st, FIN_BICG_OMEGA), g3);
+    k_bicg_update(ex, n, x.p, r.p, y.p, z.p, s.p, t.p, r0.p, pool.site(S_RES, d_st, FIN_BICG_RES),
+                  g1);
+}
+
+void Krylov::enqueueIteration()
+{
+    if (method == Method::PCG)
+        enqueuePcgIteration();
+    else
+        enqueueBicgIteration();
+}
+
+void Krylov::runIterations()
+{
+    if (useGraph && !graphExec) {
+        UNAP_CK(cudaStreamBeginCapture(ex.s, cudaStreamCaptureModeThreadLocal));
+        enqueueIteration();
+        UNAP_CK(cudaStreamEndCapture(ex.s, &graph));
+        UNAP_CK(cudaGraphInstantiate(&graphExec, graph, 0));
+    }
+    int batch = 1;
+    int launched = 0;
+    for (;;) {
+        for (int k = 0; k < batch; ++k) {
+            if (useGraph)
+                UNAP_CK(cudaGraphLaunch(graphExec, ex.s));
+            else
+                enqueueIteration();
+        }
+        launched += batch;
+        UNAP_CK(cudaGetLastError());
+        readState();
+        if (h_st->done || h_st->singular) break;
+        if (launched > maxIter + 2) break;  // safety: every iteration advances nIter
+        batch = std::min(batch * 2, 16);
+    }
+}
+
+SolveStats Krylov::solveDevice(double* x_ref, const double* b_ref)
+{
+    SolveStats out;
+    const Level& L = *A.L;
+    UNAP_CK(cudaEventRecord(ev0, ex.s));
+    k_to_internal<double>(ex, n, L.d_perm.p, x_ref, x.p);
+    k_to_internal<double>(ex, n, L.d_perm.p, b_ref, b.p);
+    initState();
+    Rows<double> Ar = rows64(L);
+    if (method == Method::PCG) {
+        // PCG.cpp:61-75: r = b - A x, initialResidual = normFactor(r)
+        k_residual<double>(ex, Ar, x.p, b.p, r.p, pool.site(S_INIT, d_st, FIN_INIT_RES), Gate{});
+    } else {
+        // PBiCGStab.cpp:72-91: yA = A x; r = r0 = b - yA
+        k_spmv<double>(ex, Ar, x.p, y.p, nullptr, RSpec{}, Gate{});
+        k_bicg_init(ex, n, b.p, y.p, r.p, r0.p, pool.site(S_INIT, d_st, FIN_BICG_INIT));
+    }
+    if (n > 0) {
+        for (;;) {
+            runIterations();
+            if (!trueResidualRestart || h_st->singular || !h_st->converged) break;
+            // true residual check: restart from b - A x if the recurrence drifted
+            k_residual<double>(ex, Ar, x.p, b.p, z.p, pool.site(S_TRUE, d_st, FIN_TRUE_RES),
+                               Gate{});
+            readState();
+            double tr = h_st->trueRes;
+            bool ok = (tr < tol) || (relTol > 1e-37 && tr <= relTol * h_st->initRes);
+            if (ok || h_st->nIter >= maxIter) break;
+            UNAP_CK(cudaMemcpyAsync(r.p, z.p, sizeof(double) * (size_t)n,
+                                    cudaMemcpyDeviceToDevice, ex.s));
+            h_st->done = 0;
+            h_st->converged = 0;
+            h_st->first = 1;
+            h_st->finalRes = tr;
+            h_st->wArA = 1.0e37;
+            UNAP_CK(cudaMemcpyAsync(d_st, h_st, sizeof(KState), cudaMemcpyHostToDevice, ex.s));
+        }
+    }
+    k_to_reference<double>(ex, n, L.d_perm.p, x.p, x_ref);
+    UNAP_CK(cudaEventRecord(ev1, ex.s));
+    readState();
+    float ms = 0;
+    UNAP_CK(cudaEventElapsedTime(&ms, ev0, ev1));
+    out.seconds = ms * 1e-3;
+    out.nIter = h_st->nIter;
+    out.initRes = h_st->initRes;
+    out.finalRes = h_st->finalRes;
+    out.trueRes = h_st->trueRes;
+    out.converged = h_st->converged;
+    out.singular = h_st->singular;
+    out.status = h_st->status;
+    return out;
+}
+
+SolveStats Krylov::solveHost(double* xh, const double* bh)
+{
+    DevArray<double> dx((size_t)n), db((size_t)n);
+    dx.upload(xh, (size_t)n, ex.s);
+    db.upload(bh, (size_t)n, ex.s);
+    SolveStats st = solveDevice(dx.p, db.p);
+    if (n) UNAP_CK(cudaMemcpyAsync(xh, dx.p, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, ex.s));
+    UNAP_CK(cudaStreamSynchronize(ex.s));
+    return st;
+}
+
+// ---- dense SPD inverse (coarsest level) --------------------------------------
+// Cholesky A = L L^T column by column, L^-1 by forward substitution,
+// A^-1 = L^-T L^-1; every sum runs over ascending index from 0 (same
+// operation order as the oracle's restatement, so both produce the same
+// bits).
+bool dense_spd_inverse(int n, const std::vector<double>& A, std::vector<double>& inv)
+{
+    const size_t N = (size_t)n;
+    std::vector<double> L(N * N, 0.0), Li(N * N, 0.0);
+    inv.assign(N * N, 0.0);
+    for (int j = 0; j < n; ++j) {
+        double s = A[(size_t)j * N + j];
+        for (int k = 0; k < j; ++k) s -= L[(size_t)j * N + k] * L[(size_t)j * N + k];
+        if (!(s > 0.0)) return false;
+        double djj = std::sqrt(s);
+        L[(size_t)j * N + j] = djj;
+        for (int i = j + 1; i < n; ++i) {
+            double t = A[(size_t)i * N + j];
+            const double* Li_ = &L[(size_t)i * N];
+            const double* Lj_ = &L[(size_t)j * N];
+            for (int k = 0; k < j; ++k) t -= Li_[k] * Lj_[k];
+            L[(size_t)i * N + j] = t / djj;
+        }
+    }
+    for (int j = 0; j < n; ++j) {
+        Li[(size_t)j * N + j] = 1.0 / L[(size_t)j * N + j];
+        for (int i = j + 1; i < n; ++i) {
+            double t = 0.0;
+            for (int k = j; k < i; ++k) t += L[(size_t)i * N + k] * Li[(size_t)k * N + j];
+            Li[(size_t)i * N + j] = -t / L[(size_t)i * N + i];
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j <= i; ++j) {
+            double t = 0.0;
+            for (int k = i; k < n; ++k) t += Li[(size_t)k * N + i] * Li[(size_t)k * N + j];
+            inv[(size_t)i * N + j] = t;
+            inv[(size_t)j * N + i] = t;
+        }
+    }
+    return true;
+}
+
+}  // namespace unapgpu

@@ -1,0 +1,88 @@
+// Host-side engine: matrices, preconditioners and Krylov drivers on one GPU.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "kernels.hpp"
+
+namespace unapgpu {
+
+struct SolveStats {
+    int nIter = 0;
+    double initRes = 0, finalRes = 0, trueRes = -1;
+    int converged = 0, singular = 0, status = 0;
+    double seconds = 0;  // device time of the solve (CUDA events)
+};
+
+// A device-resident LDU matrix (one system).  The host copy keeps the
+// reference layout; the device Level holds the internal order and SELL rows.
+class Matrix {
+public:
+    Matrix(HostLdu&& h, cudaStream_t s);
+    ~Matrix();
+    HostLdu host;
+    std::unique_ptr<Level> L;
+    cudaStream_t stream;
+    bool ownsStream = false;
+    int n() const { return host.n; }
+    // replace the coefficients (same addressing)
+    void setValues(const double* diag, const double* upper, const double* lower);
+};
+
+// Preconditioner interface: w = M^-1 r on internal-order vectors.
+class Precond {
+public:
+    virtual ~Precond() = default;
+    // true when apply() also reduces w.r into `site` and finalizes with `fin`
+    virtual bool fusesDot() const { return false; }
+    virtual void apply(const Exec& ex, const double* r, double* w, const RedPool* pool, int site,
+                       KState* st, int fin, Gate g) = 0;
+};
+
+std::unique_ptr<Precond> make_ldu_precond(int type, Matrix& A);  // 1 Diag, 2 DIC, 3 DILU, else none
+
+enum class Method { PCG, PBiCGStab };
+
+// Krylov driver with device-resident scalars and CUDA-graph iterations.
+class Krylov {
+public:
+    Krylov(Matrix& A, Precond* P, Method m);
+    ~Krylov();
+    double tol = 0.0, relTol = 1e-6;
+    int maxIter = 1000, minIter = 0;
+    bool flexible = false;   // PCG only
+    bool trueResidualRestart = false;  // re-check ||b - Ax|| and restart if needed
+    bool useGraph = true;
+    // solve on device vectors in reference order (x in/out, b in)
+    SolveStats solveDevice(double* x_ref, const double* b_ref);
+    // solve on host vectors (copies in and out)
+    SolveStats solveHost(double* x, const double* b);
+    Matrix& A;
+
+private:
+    Precond* P;
+    Method method;
+    Exec ex;
+    int n;
+    DevArray<double> x, b, r, z, p, q, r0, y, Ay, s, t, zz;
+    DevArray<double> hx_ref;  // staging for host solves
+    KState* d_st = nullptr;
+    KState* h_st = nullptr;   // pinned
+    RedPool pool;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graphExec = nullptr;
+    cudaEvent_t ev0, ev1;
+    void enqueueIteration();
+    void enqueuePcgIteration();
+    void enqueueBicgIteration();
+    void initState();
+    void runIterations();
+    void readState();
+};
+
+// Dense FP64 SPD inverse by Cholesky (row-major in, row-major out).
+// Returns false when the matrix is not positive definite.
+bool dense_spd_inverse(int n, const std::vector<double>& A, std::vector<double>& inv);
+
+}  // namespace unapgpu

@@ -1,0 +1,950 @@
+// sm_103a kernels of the UNAP solve path.  Everything here is bandwidth- or
+// latency-bound sparse work (no tensor-core shapes): SELL-32 row gathers with
+// coalesced index/value loads, wavefront-scheduled triangular sweeps, and
+// vector updates with fused warp-shuffle reductions.
+//
+// Reductions are deterministic and launch-free: each block reduces with a
+// fixed shuffle tree, the last block of a launch (ticket counter) sums the
+// block partials in a fixed order into a per-launch slot, and the last launch
+// of a site sums its slots and runs a finalize step on the solver state
+// (alpha, beta, residual norm, convergence test) in device memory.
+//
+// The library is compiled with --fmad=false so that every product and sum
+// rounds separately, as the reference's loops do on the CPU.
+#include <cmath>
+
+#include "kernels.hpp"
+
+namespace unapgpu {
+
+#define SMALL_D 1.0e-37
+
+template <class T>
+__device__ __forceinline__ T ldg(const T* p)
+{
+    return __ldg(p);
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Fixed-tree block sum of K values; the result is valid in thread 0.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K])
+{
+    __shared__ double sm[K][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) sm[k][wid] = v[k];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double t = lane < nw ? sm[k][lane] : 0.0;
+            v[k] = warp_sum(t);
+        }
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ bool gate_closed(const Gate& g)
+{
+    if (!g.st) return false;
+    if ((g.mask & 1) && g.st->done) return true;
+    if ((g.mask & 2) && g.st->early) return true;
+    return false;
+}
+
+// --- finalize operations (run by one thread) -----------------------------
+
+// solverPerformance::checkConvergence, unapMatrixTest.cpp:3-31
+__device__ __forceinline__ int check_conv(double fin, double init, double tol, double rel,
+                                          int iter, int minIter)
+{
+    return ((fin < tol || (rel > SMALL_D && fin <= rel * init)) && iter >= minIter) ? 1 : 0;
+}
+
+// do { ... } while (++nIter < maxIter && !checkConvergence(...)),
+// PCG.cpp:167-180 / PBiCGStab.cpp:443-456 / MGSolve.cpp:161-176
+__device__ __forceinline__ void iteration_end(KState* st)
+{
+    st->nIter++;
+    if (!(st->nIter < st->maxIter)) {
+        st->done = 1;
+        return;
+    }
+    st->converged = check_conv(st->finalRes, st->initRes, st->tol, st->relTol, st->nIter,
+                               st->minIter);
+    if (st->converged) st->done = 1;
+}
+
+// rA0rA update at the top of a PBiCGStab iteration (PBiCGStab.cpp:155-243)
+__device__ __forceinline__ void bicg_rr(KState* st, double rr)
+{
+    st->rA0rAold = st->rA0rA;
+    st->rA0rA = rr;
+    if (!(fabs(st->rA0rA) > SMALL_D)) {
+        st->singular = 1;
+        st->done = 1;
+        return;
+    }
+    if (st->first) {
+        st->useBeta = 0;
+        st->first = 0;
+    } else {
+        st->useBeta = 1;
+        st->beta = (st->rA0rA / st->rA0rAold) * (st->alpha / st->omega);
+    }
+}
+
+template <int K>
+__device__ void finalize(const RSpec& r, const double (&s)[K])
+{
+    KState* st = r.st;
+    switch (r.fin) {
+    case FIN_INIT_RES:
+        st->initRes = sqrt(s[0]) + SMALL_D;
+        st->finalRes = st->initRes;
+        break;
+    case FIN_RES_ONLY: st->finalRes = sqrt(s[0]) + SMALL_D; break;
+    case FIN_TRUE_RES: st->trueRes = sqrt(s[0]) + SMALL_D; break;
+    case FIN_PCG_WR: {
+        st->wArAold = st->wArA;
+        st->wArA = s[0];
+        // checkSingularity(mag(wArA)), PCG.cpp:107-117
+        if (!(fabs(st->wArA) > SMALL_D)) {
+            st->singular = 1;
+            st->done = 1;
+            break;
+        }
+        if (st->first) {
+            st->useBeta = 0;
+            st->first = 0;
+        } else {
+            st->useBeta = 1;
+            if (st->flexible && K > 1)
+                st->beta = (-st->alpha * s[K > 1 ? 1 : 0]) / st->wArAold;
+            else
+                st->beta = st->wArA / st->wArAold;
+        }
+        break;
+    }
+    case FIN_PCG_ALPHA:
+        st->wApA = s[0];
+        st->alpha = st->wArA / st->wApA;
+        break;
+    case FIN_PCG_RES:
+        st->finalRes = sqrt(s[0]) + SMALL_D;
+        iteration_end(st);
+        break;
+    case FIN_MG_RES:
+        st->finalRes = sqrt(s[0]) + SMALL_D;
+        iteration_end(st);
+        break;
+    case FIN_BICG_INIT:
+        // initial residual; s[1] = rA0.rA of the first iteration
+        st->initRes = sqrt(s[0]) + SMALL_D;
+        st->finalRes = st->initRes;
+        st->rA0rA = 0.0;
+        bicg_rr(st, s[K > 1 ? 1 : 0]);
+        break;
+    case FIN_BICG_ALPHA: st->alpha = st->rA0rA / s[0]; break;
+    case FIN_BICG_S:
+        st->finalRes = sqrt(s[0]) + SMALL_D;
+        // PBiCGStab.cpp:298-349: converged on ||s|| -> x += alpha y,
+        // nIterations()++, return.  `early` gates the rest of the iteration.
+        if (check_conv(st->finalRes, st->initRes, st->tol, st->relTol, st->nIter + 1,
+                       st->minIter)) {
+            st->converged = 1;
+            st->early = 1;
+            st->nIter++;
+        } else {
+            st->converged = 0;
+        }
+        break;
+    case FIN_BICG_OMEGA:
+        st->tAtA = s[0];
+        st->tAsA = s[1 < K ? 1 : 0];
+        st->omega = st->tAsA / st->tAtA;
+        break;
+    case FIN_BICG_RES:
+        if (st->early) {  // half-step exit finished: x += alpha y is done
+            st->done = 1;
+            break;
+        }
+        // ||r|| and the loop test; s[1] = rA0.r is the next iteration's
+        // rA0rA (PBiCGStab.cpp:155-196), tested for singularity only when the
+        // loop continues
+        st->finalRes = sqrt(s[0]) + SMALL_D;
+        iteration_end(st);
+        if (!st->done) bicg_rr(st, s[K > 1 ? 1 : 0]);
+        break;
+    default: break;
+    }
+}
+
+// Two-level deterministic reduction + finalize.
+template <int K>
+__device__ __forceinline__ void reduce_and_finalize(double (&v)[K], const RSpec& r)
+{
+    block_sum<K>(v);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) r.blockPart[blockIdx.x * K + k] = v[k];
+    }
+    __threadfence();
+    __shared__ int amLast;
+    if (threadIdx.x == 0) amLast = (atomicAdd(r.ticket, 1u) == gridDim.x - 1) ? 1 : 0;
+    __syncthreads();
+    if (!amLast) return;
+    __threadfence();
+    double s[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) s[k] += __ldcg(r.blockPart + b * K + k);
+    }
+    block_sum<K>(s);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) r.launchAcc[r.slot * K + k] = s[k];
+        *r.ticket = 0u;
+        if (r.fin != FIN_STORE && r.fin != FIN_NONE) {
+            double t[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) t[k] = 0.0;
+            for (int j = 0; j < r.nSlots; ++j) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) t[k] += __ldcg(r.launchAcc + j * K + k);
+            }
+            finalize<K>(r, t);
+        }
+        __threadfence();
+    }
+}
+
+// --------------------------------------------------------------------------
+// SELL-32 row helpers
+// --------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T row_apply(const Rows<T>& A, int r, const T* __restrict__ x)
+{
+    const int info = ldg(A.rowInfo + r);
+    const int len = info & 0xffff;
+    const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
+    // lduMatrixSpMV.cpp:83-92: Apsi = 0; += diag psi; then faces in face order
+    T acc = T(0);
+    acc += ldg(A.diag + r) * ldg(x + r);
+    for (int j = 0; j < len; ++j) {
+        const int e = base + 32 * j;
+        acc += ldg(A.val + e) * ldg(x + ldg(A.col + e));
+    }
+    return acc;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) spmv_kernel(Rows<T> A, const T* __restrict__ x,
+                                                      T* __restrict__ y, const T* dotWith,
+                                                      RSpec red, Gate g)
+{
+    if (gate_closed(g)) return;
+    double v[1] = {0.0};
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < A.n; r += gridDim.x * blockDim.x) {
+        T a = row_apply(A, r, x);
+        y[r] = a;
+        if (dotWith) v[0] += (double)a * (double)dotWith[r];
+    }
+    if (red.blockPart) reduce_and_finalize<1>(v, red);
+}
+
+template <class T>
+void k_spmv(const Exec& ex, const Rows<T>& A, const T* x, T* y, const T* dotWith, RSpec red,
+            Gate g)
+{
+    if (A.n <= 0) return;
+    spmv_kernel<T><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, y, red.blockPart ? dotWith : nullptr,
+                                                      red, g);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) residual_kernel(Rows<T> A, const T* __restrict__ x,
+                                                          const T* __restrict__ b,
+                                                          T* __restrict__ r, RSpec red, Gate g)
+{
+    if (gate_closed(g)) return;
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+        T a = row_apply(A, i, x);
+        T ri = ldg(b + i) - a;
+        r[i] = ri;
+        v[0] += (double)ri * (double)ri;
+    }
+    if (red.blockPart) reduce_and_finalize<1>(v, red);
+}
+
+template <class T>
+void k_residual(const Exec& ex, const Rows<T>& A, const T* x, const T* b, T* r, RSpec red, Gate g)
+{
+    if (A.n <= 0) return;
+    residual_kernel<T><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, b, r, red, g);
+}
+
+// --------------------------------------------------------------------------
+// Gauss-Seidel (lduGaussSeidelSmoother.cpp:40-79) on one wavefront.
+// x_c = (b_c - sum_low val x_l - sum_up val x_u) / D_c, lower-side faces
+// first, each side in ascending face order, exactly the reference's
+// bPrime accumulation followed by the owner-face loop.
+// --------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(kBlock) gs_kernel(Rows<T> A, T* x, const T* __restrict__ b,
+                                                    int r0, int r1, int skipUpper, Gate g)
+{
+    if (gate_closed(g)) return;
+    for (int r = r0 + blockIdx.x * blockDim.x + threadIdx.x; r < r1;
+         r += gridDim.x * blockDim.x) {
+        const int info = ldg(A.rowInfo + r);
+        const int len = info & 0xffff;
+        const int nLow = info >> 16;
+        const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
+        T acc = ldg(b + r);
+        for (int j = 0; j < nLow; ++j) {
+            const int e = base + 32 * j;
+            acc -= ldg(A.val + e) * x[ldg(A.col + e)];
+        }
+        if (!skipUpper) {
+            for (int j = nLow; j < len; ++j) {
+                const int e = base + 32 * j;
+                acc -= ldg(A.val + e) * x[ldg(A.col + e)];
+            }
+        }
+        x[r] = acc / ldg(A.diag + r);
+    }
+}
+
+template <class T>
+void k_gs_rows(const Exec& ex, const Rows<T>& A, T* x, const T* b, int r0, int r1, bool skipUpper,
+               Gate g)
+{
+    if (r1 <= r0) return;
+    gs_kernel<T><<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, x, b, r0, r1, skipUpper ? 1 : 0, g);
+}
+
+template <class T>
+void gs_sweep(const Exec& ex, const Level& L, const Rows<T>& A, T* x, const T* b, bool backward,
+              bool xIsZero, Gate g)
+{
+    const int W = L.nWave;
+    for (int k = 0; k < W; ++k) {
+        int w = backward ? W - 1 - k : k;
+        k_gs_rows<T>(ex, A, x, b, L.waveStart[w], L.waveStart[w + 1], xIsZero && !backward, g);
+    }
+}
+
+// --------------------------------------------------------------------------
+// DIC / DILU
+// --------------------------------------------------------------------------
+
+// lduDICPrecond::calcReciprocalD (lduDICPrecond.cpp:15-42) and the DILU
+// variant (lduDILUPrecond.cpp:15-43) on one wavefront:
+// dfac_c = D_c - sum over lower-side faces (asc) of (c1 c2) / dfac_l
+__global__ void __launch_bounds__(kBlock) factor_kernel(Rows<double> A, const double* c1,
+                                                        const double* c2, double* dfac, int r0,
+                                                        int r1)
+{
+    for (int r = r0 + blockIdx.x * blockDim.x + threadIdx.x; r < r1;
+         r += gridDim.x * blockDim.x) {
+        const int info = ldg(A.rowInfo + r);
+        const int nLow = info >> 16;
+        const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
+        double d = ldg(A.diag + r);
+        for (int j = 0; j < nLow; ++j) {
+            const int e = base + 32 * j;
+            d -= ldg(c1 + e) * ldg(c2 + e) / dfac[ldg(A.col + e)];
+        }
+        dfac[r] = d;
+    }
+}
+
+__global__ void recip_kernel(int n, const double* __restrict__ d, double* __restrict__ rD)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        rD[i] = 1.0 / d[i];
+}
+
+void dic_factor(const Exec& ex, const Level& L, bool dilu, double* dfac, double* rD)
+{
+    Rows<double> A = rows64(L);
+    // DIC: upper * upper; DILU: upper * lower.  On the lower side of a row the
+    // face's upper coefficient is valT and its lower coefficient is val.
+    const double* c1 = A.valT;
+    const double* c2 = dilu ? A.val : A.valT;
+    for (int w = 0; w < L.nWave; ++w) {
+        int r0 = L.waveStart[w], r1 = L.waveStart[w + 1];
+        if (r1 > r0) factor_kernel<<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, c1, c2, dfac, r0, r1);
+    }
+    if (L.n) recip_kernel<<<ex.grid(L.n), kBlock, 0, ex.s>>>(L.n, dfac, rD);
+}
+
+// forward sweep (lduDICPrecond.cpp:63-71; DILU in losort order,
+// lduDILUPrecond.cpp:70-80): w_c = rD_c r_c - sum_low (rD_c coef) w_l
+__global__ void __launch_bounds__(kBlock) dic_fwd_kernel(Rows<double> A, const double* coef,
+                                                         const double* __restrict__ rD,
+                                                         const double* __restrict__ rr,
+                                                         double* w, int r0, int r1, Gate g)
+{
+    if (gate_closed(g)) return;
+    for (int r = r0 + blockIdx.x * blockDim.x + threadIdx.x; r < r1;
+         r += gridDim.x * blockDim.x) {
+        const int info = ldg(A.rowInfo + r);
+        const int nLow = info >> 16;
+        const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
+        const double rd = ldg(rD + r);
+        double acc = rd * ldg(rr + r);
+        for (int j = 0; j < nLow; ++j) {
+            const int e = base + 32 * j;
+            acc -= rd * ldg(coef + e) * w[ldg(A.col + e)];
+        }
+        w[r] = acc;
+    }
+}
+
+// backward sweep (lduDICPrecond.cpp:73-76): faces in reverse order,
+// w_c -= (rD_c upper) w_u; sums w.r for the PCG/PBiCGStab dot product
+__global__ void __launch_bounds__(kBlock) dic_bwd_kernel(Rows<double> A,
+                                                         const double* __restrict__ rD,
+                                                         const double* __restrict__ rr,
+                                                         double* w, int r0, int r1, RSpec red,
+                                                         Gate g)
+{
+    if (gate_closed(g)) return;
+    double v[1] = {0.0};
+    for (int r = r0 + blockIdx.x * blockDim.x + threadIdx.x; r < r1;
+         r += gridDim.x * blockDim.x) {
+        const int info = ldg(A.rowInfo + r);
+        const int len = info & 0xffff;
+        const int nLow = info >> 16;
+        const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
+        const double rd = ldg(rD + r);
+        double acc = w[r];
+        for (int j = len - 1; j >= nLow; --j) {
+            const int e = base + 32 * j;
+            acc -= rd * ldg(A.val + e) * w[ldg(A.col + e)];
+        }
+        w[r] = acc;
+        v[0] += acc * ldg(rr + r);
+    }
+    if (red.blockPart) reduce_and_finalize<1>(v, red);
+}
+
+void dic_apply(const Exec& ex, const Level& L, bool dilu, const double* rD, const double* r,
+               double* w, const RedPool* pool, int site, KState* st, int fin, Gate g)
+{
+    Rows<double> A = rows64(L);
+    const double* coef = dilu ? A.val : A.valT;  // DIC uses upper on the lower side
+    const int W = L.nWave;
+    for (int k = 0; k < W; ++k) {
+        int r0 = L.waveStart[k], r1 = L.waveStart[k + 1];
+        if (r1 > r0)
+            dic_fwd_kernel<<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, coef, rD, r, w, r0, r1, g);
+    }
+    // backward: one launch slot per non-empty wavefront
+    int nonEmpty = 0;
+    for (int k = 0; k < W; ++k) nonEmpty += L.waveStart[k + 1] > L.waveStart[k];
+    int slot = 0;
+    for (int k = W - 1; k >= 0; --k) {
+        int r0 = L.waveStart[k], r1 = L.waveStart[k + 1];
+        if (r1 <= r0) continue;
+        RSpec red;
+        if (pool) red = pool->site(site, st, slot == nonEmpty - 1 ? fin : FIN_STORE, slot, nonEmpty);
+        dic_bwd_kernel<<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, rD, r, w, r0, r1, red, g);
+        ++slot;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) diag_apply_kernel(int n, const double* __restrict__ rD,
+                                                            const double* __restrict__ r,
+                                                            double* __restrict__ w, RSpec red,
+                                                            Gate g)
+{
+    if (gate_closed(g)) return;
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double wi = rD ? rD[i] * r[i] : r[i];
+        w[i] = wi;
+        v[0] += wi * r[i];
+    }
+    if (red.blockPart) reduce_and_finalize<1>(v, red);
+}
+
+void diag_apply(const Exec& ex, int n, const double* rD, const double* r, double* w, RSpec red,
+                Gate g)
+{
+    if (n <= 0) return;
+    diag_apply_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, rD, r, w, red, g);
+}
+
+// --------------------------------------------------------------------------
+// PCG vector kernels (PCG.cpp:119-151)
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) pcg_direction_kernel(int n, const double* __restrict__ w,
+                                                               double* __restrict__ p,
+                                                               const KState* st, Gate g)
+{
+    if (gate_closed(g)) return;
+    const bool useBeta = st->useBeta;
+    const double beta = st->beta;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        p[i] = useBeta ? w[i] + beta * p[i] : w[i];
+}
+
+void k_pcg_direction(const Exec& ex, int n, const double* w, double* p, const KState* st, Gate g)
+{
+    if (n <= 0) return;
+    pcg_direction_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, w, p, st, g);
+}
+
+__global__ void __launch_bounds__(kBlock) pcg_update_kernel(int n, double* __restrict__ x,
+                                                            double* __restrict__ r,
+                                                            const double* __restrict__ p,
+                                                            const double* __restrict__ q,
+                                                            RSpec red, Gate g)
+{
+    if (gate_closed(g)) return;
+    const double alpha = red.st->alpha;
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        x[i] += alpha * p[i];
+        double ri = r[i] - alpha * q[i];
+        r[i] = ri;
+        v[0] += ri * ri;
+    }
+    reduce_and_finalize<1>(v, red);
+}
+
+void k_pcg_update(const Exec& ex, int n, double* x, double* r, const double* p, const double* q,
+                  RSpec red, Gate g)
+{
+    if (n <= 0) return;
+    pcg_update_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, x, r, p, q, red, g);
+}
+
+__global__ void __launch_bounds__(kBlock) dot2_kernel(int n, const double* __restrict__ a,
+                                                      const double* __restrict__ b,
+                                                      const double* __restrict__ c,
+                                                      const double* __restrict__ d, RSpec red,
+                                                      Gate g)
+{
+    if (gate_closed(g)) return;
+    double v[2] = {0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        v[0] += a[i] * b[i];
+        if (c) v[1] += c[i] * d[i];
+    }
+    reduce_and_finalize<2>(v, red);
+}
+
+void k_dot2(const Exec& ex, int n, const double* a, const double* b, const double* c,
+            const double* d, RSpec red, Gate g)
+{
+    dot2_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, a, b, c, d, red, g);
+}
+
+// --------------------------------------------------------------------------
+// PBiCGStab vector kernels (PBiCGStab.cpp:83-396, x86 branches)
+// --------------------------------------------------------------------------
+
+// r = b - Ax, r0 = r; sums r.r and r0.r
+__global__ void __launch_bounds__(kBlock) bicg_init_kernel(int n, const double* __restrict__ b,
+                                                           const double* __restrict__ Ax,
+                                                           double* __restrict__ r,
+                                                           double* __restrict__ r0, RSpec red)
+{
+    double v[2] = {0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double ri = b[i] - Ax[i];
+        r[i] = ri;
+        r0[i] = ri;
+        v[0] += ri * ri;
+        v[1] += ri * ri;
+    }
+    reduce_and_finalize<2>(v, red);
+}
+
+void k_bicg_init(const Exec& ex, int n, const double* b, const double* Ax, double* r, double* r0,
+                 RSpec red)
+{
+    bicg_init_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, b, Ax, r, r0, red);
+}
+
+// p = r (first) or p = r + beta (p - omega Ay)
+__global__ void __launch_bounds__(kBlock) bicg_direction_kernel(int n,
+                                                                const double* __restrict__ r,
+                                                                const double* __restrict__ Ay,
+                                                                double* __restrict__ p,
+                                                                const KState* st, Gate g)
+{
+    if (gate_closed(g)) return;
+    const bool useBeta = st->useBeta;
+    const double beta = st->beta, omega = st->omega;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        p[i] = useBeta ? r[i] + beta * (p[i] - omega * Ay[i]) : r[i];
+}
+
+void k_bicg_direction(const Exec& ex, int n, const double* r, const double* Ay, double* p,
+                      const KState* st, Gate g)
+{
+    if (n <= 0) return;
+    bicg_direction_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, r, Ay, p, st, g);
+}
+
+// s = r - alpha Ay; sums s.s
+__global__ void __launch_bounds__(kBlock) bicg_s_kernel(int n, const double* __restrict__ r,
+                                                        const double* __restrict__ Ay,
+                                                        double* __restrict__ s, RSpec red, Gate g)
+{
+    if (gate_closed(g)) return;
+    const double alpha = red.st->alpha;
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double si = r[i] - alpha * Ay[i];
+        s[i] = si;
+        v[0] += si * si;
+    }
+    reduce_and_finalize<1>(v, red);
+}
+
+void k_bicg_s(const Exec& ex, int n, const double* r, const double* Ay, double* s, RSpec red,
+              Gate g)
+{
+    bicg_s_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, r, Ay, s, red, g);
+}
+
+// early exit: x += alpha y; else x += alpha y + omega z, r = s - omega t;
+// sums r.r and r0.r (the next iteration's rA0rA)
+__global__ void __launch_bounds__(kBlock) bicg_update_kernel(int n, double* __restrict__ x,
+                                                             double* __restrict__ r,
+                                                             const double* __restrict__ y,
+                                                             const double* __restrict__ z,
+                                                             const double* __restrict__ s,
+                                                             const double* __restrict__ t,
+                                                             const double* __restrict__ r0,
+                                                             RSpec red, Gate g)
+{
+    if (gate_closed(g)) return;
+    KState* st = red.st;
+    const double alpha = st->alpha, omega = st->omega;
+    double v[2] = {0.0, 0.0};
+    if (st->early) {
+        // PBiCGStab.cpp:310-349: x += alpha y and return (the iteration
+        // count was advanced by the ||s|| finalize; the finalize of this
+        // launch's reduction, run after every block has updated x, sets done)
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            x[i] += alpha * y[i];
+    } else {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+             i += gridDim.x * blockDim.x) {
+            x[i] += alpha * y[i] + omega * z[i];
+            double ri = s[i] - omega * t[i];
+            r[i] = ri;
+            v[0] += ri * ri;
+            v[1] += r0[i] * ri;
+        }
+    }
+    reduce_and_finalize<2>(v, red);
+}
+
+void k_bicg_update(const Exec& ex, int n, double* x, double* r, const double* y, const double* z,
+                   const double* s, const double* t, const double* r0, RSpec red, Gate g)
+{
+    bicg_update_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, x, r, y, z, s, t, r0, red,
+                                                                    g);
+}
+
+// --------------------------------------------------------------------------
+// permutations, transfers, dense coarsest solve, helpers
+// --------------------------------------------------------------------------
+template <class T>
+__global__ void to_internal_kernel(int n, const int* __restrict__ perm, const T* __restrict__ in,
+                                   T* __restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = in[perm[i]];
+}
+
+template <class T>
+__global__ void to_reference_kernel(int n, const int* __restrict__ perm,
+                                    const T* __restrict__ in, T* __restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[perm[i]] = in[i];
+}
+
+template <class T>
+void k_to_internal(const Exec& ex, int n, const int* perm, const T* in, T* out)
+{
+    if (n > 0) to_internal_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, perm, in, out);
+}
+
+template <class T>
+void k_to_reference(const Exec& ex, int n, const int* perm, const T* in, T* out)
+{
+    if (n > 0) to_reference_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, perm, in, out);
+}
+
+// restrictField (unapMatrix.hpp:378-407) in gather form: children ascending
+template <class T>
+__global__ void restrict_kernel(int nc, const int* __restrict__ cs, const int* __restrict__ ch,
+                                const T* __restrict__ fine, T* __restrict__ coarse, Gate g)
+{
+    if (gate_closed(g)) return;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        T s = T(0);
+        for (int k = cs[c]; k < cs[c + 1]; ++k) s += fine[ch[k]];
+        coarse[c] = s;
+    }
+}
+
+template <class T>
+void k_restrict(const Exec& ex, int nCoarse, const int* childStart, const int* child,
+                const T* fine, T* coarse, Gate g)
+{
+    if (nCoarse > 0)
+        restrict_kernel<T><<<ex.grid(nCoarse), kBlock, 0, ex.s>>>(nCoarse, childStart, child, fine,
+                                                                  coarse, g);
+}
+
+template <class T>
+__global__ void prolong_add_kernel(int nf, const int* __restrict__ cmap,
+                                   const T* __restrict__ coarse, T* __restrict__ fine, Gate g)
+{
+    if (gate_closed(g)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x)
+        fine[i] += coarse[cmap[i]];
+}
+
+template <class T>
+void k_prolong_add(const Exec& ex, int nFine, const int* cmap, const T* coarse, T* fine, Gate g)
+{
+    if (nFine > 0)
+        prolong_add_kernel<T><<<ex.grid(nFine), kBlock, 0, ex.s>>>(nFine, cmap, coarse, fine, g);
+}
+
+// Dense coarsest solve: x_i = sum_j Minv[i][j] b_j, j ascending, FP64.
+// b is staged in shared memory as FP64; thread i walks column-major Minv so
+// a warp reads 32 consecutive rows of one column per step.
+template <class T>
+__global__ void dense_apply_kernel(int n, const double* __restrict__ M, const T* __restrict__ b,
+                                   T* __restrict__ x, Gate g)
+{
+    if (gate_closed(g)) return;
+    extern __shared__ double sb[];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = (double)b[j];
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double t = 0.0;
+        for (int j = 0; j < n; ++j) t += ldg(M + (size_t)j * n + i) * sb[j];
+        x[i] = (T)t;
+    }
+}
+
+template <class T>
+void k_dense_apply(const Exec& ex, int n, const double* MinvColMajor, const T* b, T* x, Gate g)
+{
+    if (n <= 0) return;
+    int threads = 64;
+    int blocks = div_up(n, threads);
+    dense_apply_kernel<T><<<blocks, threads, (size_t)n * sizeof(double), ex.s>>>(n, MinvColMajor,
+                                                                               b, x, g);
+}
+
+template <class T>
+__global__ void fill_kernel(long long n, T* x, T v)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        x[i] = v;
+}
+
+template <class T>
+void k_fill(const Exec& ex, long long n, T* x, T v)
+{
+    if (n > 0) fill_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, x, v);
+}
+
+__global__ void d2f_kernel(int n, const double* __restrict__ in, float* __restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+__global__ void f2d_kernel(int n, const float* __restrict__ in, double* __restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+void k_d2f(const Exec& ex, int n, const double* in, float* out)
+{
+    if (n > 0) d2f_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, in, out);
+}
+
+void k_f2d(const Exec& ex, int n, const float* in, double* out)
+{
+    if (n > 0) f2d_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, in, out);
+}
+
+void k_axpy_f2d(const Exec& ex, int n, const float* in, double* out) { k_f2d(ex, n, in, out); }
+
+// scalingFactor.cpp:35-64: sums source.field and Acf.field, then a Jacobi
+// step field += (source - Acf)/D
+template <class T>
+__global__ void __launch_bounds__(kBlock) scaling_kernel(int n, const T* __restrict__ src,
+                                                         const T* __restrict__ Acf, T* field,
+                                                         const T* __restrict__ D, RSpec red,
+                                                         Gate g)
+{
+    if (gate_closed(g)) return;
+    double v[2] = {0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        T f = field[i];
+        v[0] += (double)(src[i] * f);
+        v[1] += (double)(Acf[i] * f);
+        field[i] = f + (src[i] - Acf[i]) / D[i];
+    }
+    reduce_and_finalize<2>(v, red);
+}
+
+template <class T>
+void k_scaling_sums(const Exec& ex, int n, const T* source, const T* Acf, T* field, const T* D,
+                    RSpec red, Gate g)
+{
+    scaling_kernel<T><<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, source, Acf, field, D, red,
+                                                                   g);
+}
+
+template <class T>
+__global__ void axpby_kernel(int n, T a, const T* __restrict__ x, T b, T* __restrict__ y, Gate g)
+{
+    if (gate_closed(g)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        y[i] = a * x[i] + b * y[i];
+}
+
+template <class T>
+void k_axpby(const Exec& ex, int n, T a, const T* x, T b, T* y, Gate g)
+{
+    if (n > 0) axpby_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, a, x, b, y, g);
+}
+
+// --------------------------------------------------------------------------
+Rows<double> rows64(const Level& L)
+{
+    Rows<double> A;
+    A.n = L.n;
+    A.sliceOff = L.d_sliceOff.p;
+    A.rowInfo = L.d_rowInfo.p;
+    A.col = L.d_col.p;
+    A.val = L.d_val.p;
+    A.valT = L.symm ? L.d_val.p : L.d_valT.p;
+    A.diag = L.d_diag.p;
+    return A;
+}
+
+Rows<float> rows32(const Level& L)
+{
+    Rows<float> A;
+    A.n = L.n;
+    A.sliceOff = L.d_sliceOff.p;
+    A.rowInfo = L.d_rowInfo.p;
+    A.col = L.d_col.p;
+    A.val = L.d_val32.p;
+    A.valT = L.d_val32.p;
+    A.diag = L.d_diag32.p;
+    return A;
+}
+
+void make_fp32(Level& L, cudaStream_t s)
+{
+    if (L.d_val32.p) return;
+    Exec ex;
+    ex.s = s;
+    ex.maxBlocks = device_max_blocks();
+    L.d_val32.alloc((size_t)L.nEntries);
+    L.d_diag32.alloc((size_t)L.n);
+    if (L.nEntries) d2f_kernel<<<ex.grid(L.nEntries), kBlock, 0, s>>>((int)L.nEntries, L.d_val.p, L.d_val32.p);
+    if (L.n) d2f_kernel<<<ex.grid(L.n), kBlock, 0, s>>>(L.n, L.d_diag.p, L.d_diag32.p);
+    UNAP_CK(cudaGetLastError());
+}
+
+void RedPool::init(int sites, int blocks, int launches, cudaStream_t s)
+{
+    nSites = sites;
+    maxBlocks = blocks;
+    maxLaunch = launches;
+    blockPart.alloc((size_t)sites * blocks * kRedK);
+    launchAcc.alloc((size_t)sites * launches * kRedK);
+    tickets.alloc((size_t)sites);
+    tickets.zero(s);
+}
+
+RSpec RedPool::site(int i, KState* st, int fin, int slot, int nSlots) const
+{
+    RSpec r;
+    r.blockPart = blockPart.p + (size_t)i * maxBlocks * kRedK;
+    r.launchAcc = launchAcc.p + (size_t)i * maxLaunch * kRedK;
+    r.ticket = tickets.p + i;
+    r.slot = slot;
+    r.nSlots = nSlots;
+    r.fin = fin;
+    r.st = st;
+    return r;
+}
+
+int device_max_blocks()
+{
+    static int cached = 0;
+    if (!cached) {
+        int dev = 0, sms = 0, perSm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&perSm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+        if (sms <= 0) sms = 152;
+        if (perSm <= 0) perSm = 2048;
+        cached = sms * (perSm / kBlock);
+    }
+    return cached;
+}
+
+// --------------------------------------------------------------------------
+// explicit instantiations
+// --------------------------------------------------------------------------
+#define INST(T)                                                                                   \
+    template void k_spmv<T>(const Exec&, const Rows<T>&, const T*, T*, const T*, RSpec, Gate);     \
+    template void k_residual<T>(const Exec&, const Rows<T>&, const T*, const T*, T*, RSpec, Gate); \
+    template void k_gs_rows<T>(const Exec&, const Rows<T>&, T*, const T*, int, int, bool, Gate);   \
+    template void gs_sweep<T>(const Exec&, const Level&, const Rows<T>&, T*, const T*, bool, bool, \
+                              Gate);                                                              \
+    template void k_to_internal<T>(const Exec&, int, const int*, const T*, T*);                   \
+    template void k_to_reference<T>(const Exec&, int, const int*, const T*, T*);                  \
+    template void k_restrict<T>(const Exec&, int, const int*, const int*, const T*, T*, Gate);    \
+    template void k_prolong_add<T>(const Exec&, int, const int*, const T*, T*, Gate);             \
+    template void k_dense_apply<T>(const Exec&, int, const double*, const T*, T*, Gate);          \
+    template void k_fill<T>(const Exec&, long long, T*, T);                                        \
+    template void k_scaling_sums<T>(const Exec&, int, const T*, const T*, T*, const T*, RSpec,    \
+                                    Gate);                                                        \
+    template void k_axpby<T>(const Exec&, int, T, const T*, T, T*, Gate);
+
+INST(double)
+INST(float)
+template void k_fill<int>(const Exec&, long long, int*, int);
+
+}  // namespace unapgpu

@@ -1,0 +1,228 @@
+// Internal declarations of the GB300 UNAP library (not part of the C ABI).
+//
+// Device data model, one `Level` per LDU matrix of a hierarchy:
+//
+//  * Cells are renumbered into an internal order that is level-major with
+//    respect to the forward dependency DAG of the matrix in its own
+//    numbering (cell c depends on every lower neighbour l < c, i.e. on every
+//    face f with upperAddr[f] == c).  Each wavefront is a contiguous internal
+//    range, so the forward sweeps of DIC/DILU/Gauss-Seidel walk the
+//    wavefronts in order and the backward sweeps walk them in reverse, with
+//    exactly the reference's cell-order dependencies.  Within a wavefront
+//    cells follow a locality key (BFS order on the finest level, inherited
+//    through the aggregates on coarse levels) so neighbour gathers hit L2.
+//  * Off-diagonal entries are stored as sliced ELLPACK with slices of 32 rows
+//    (SELL-32): entry j of row r lives at sliceOff[r/32] + 32*j + r%32, so a
+//    warp loads 32 consecutive column indices and values.  A row's entries
+//    are its faces in ascending face order; for owner-sorted matrices that is
+//    [faces with upperAddr == c][faces with lowerAddr == c], the split point
+//    being nLow.  Per-row summation order therefore equals the reference's
+//    face loops (lduMatrixSpMV.cpp:83-92, lduGaussSeidelSmoother.cpp:53-78,
+//    lduDICPrecond.cpp:63-76), which makes those kernels bit-identical to it.
+//  * val[e] is the matrix entry A[row][col] (lower[f] on the lower side,
+//    upper[f] on the upper side); valT[e] is the transposed coefficient
+//    (upper[f] on the lower side), needed by DIC/DILU on asymmetric storage.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace unapgpu {
+
+struct CudaError : std::runtime_error {
+    explicit CudaError(const std::string& m) : std::runtime_error(m) {}
+};
+
+#define UNAP_CK(call)                                                                     \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            throw ::unapgpu::CudaError(std::string(#call) + ": " + cudaGetErrorString(e_) + \
+                                       " at " + __FILE__ + ":" + std::to_string(__LINE__)); \
+    } while (0)
+
+void set_last_error(const std::string& msg);
+const char* last_error();
+
+template <class T>
+struct DevArray {
+    T* p = nullptr;
+    size_t n = 0;
+    DevArray() = default;
+    explicit DevArray(size_t count) { alloc(count); }
+    DevArray(const DevArray&) = delete;
+    DevArray& operator=(const DevArray&) = delete;
+    DevArray(DevArray&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevArray& operator=(DevArray&& o) noexcept
+    {
+        if (this != &o) {
+            release();
+            p = o.p;
+            n = o.n;
+            o.p = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
+    ~DevArray() { release(); }
+    void alloc(size_t count)
+    {
+        release();
+        n = count;
+        if (count) UNAP_CK(cudaMalloc((void**)&p, count * sizeof(T)));
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void upload(const T* h, size_t count, cudaStream_t s = 0)
+    {
+        if (count != n) alloc(count);
+        if (count) UNAP_CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void upload(const std::vector<T>& h, cudaStream_t s = 0) { upload(h.data(), h.size(), s); }
+    void zero(cudaStream_t s = 0)
+    {
+        if (n) UNAP_CK(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// Host copy of one LDU matrix in the reference's layout.
+struct HostLdu {
+    int n = 0, nf = 0;
+    bool symm = true;
+    std::vector<int> l, u;
+    std::vector<double> lower, diag, upper;  // lower empty when symm
+    bool oriented = true;     // lowerAddr[f] < upperAddr[f] for every face
+    bool ownerSorted = true;  // lowerAddr non-decreasing
+    const double* lowerPtr() const { return symm ? upper.data() : lower.data(); }
+    void validate();
+};
+
+// Per-matrix topology on the device (shared by FP64 and FP32 values).
+struct Level {
+    int n = 0, nf = 0;
+    bool symm = true;
+    bool sweepable = true;   // oriented && ownerSorted: DIC/DILU/GS allowed
+    int nWave = 0;           // number of forward wavefronts
+    std::vector<int> waveStart;  // nWave+1, internal row ranges
+    std::vector<int> perm;       // internal -> reference cell
+    std::vector<int> iperm;      // reference cell -> internal
+    int nSlices = 0;
+    long long nEntries = 0;      // padded SELL storage
+    int maxRowLen = 0;
+    DevArray<int> d_perm, d_iperm;
+    DevArray<int> d_sliceOff, d_rowInfo, d_col;
+    // FP64 values
+    DevArray<double> d_val, d_valT, d_diag;
+    // FP32 values (mixed precision); filled on demand
+    DevArray<float> d_val32, d_diag32;
+    // SELL positions of each face's two entries (row u: lower side, row l:
+    // upper side), kept to refresh coefficients without rebuilding topology
+    std::vector<int> entLo, entUp;
+    int version = 0;  // bumped on every coefficient update
+    size_t deviceBytes() const;
+};
+
+// Replace the FP64 coefficients of a Level (same addressing and symmetry).
+void update_level_values(Level& L, const HostLdu& A, cudaStream_t s);
+
+// Build the internal order, the SELL-32 structure and upload FP64 values.
+// `key` (optional, size n) gives the locality order inside a wavefront;
+// when empty a BFS order of the matrix graph is used.  `identityOrder`
+// keeps the reference numbering (used for the dense coarsest level).
+std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key,
+                                   bool identityOrder, cudaStream_t s);
+void make_fp32(Level& L, cudaStream_t s);
+
+// Solver state shared by the device kernels of one solve (device memory).
+// Every kernel of an iteration first checks `done` (and `early` where the
+// BiCGStab half-step exit applies) and returns at once when set, so a host
+// can enqueue or graph-launch iterations ahead of the convergence test.
+struct KState {
+    double wArA, wArAold, wApA, alpha, beta, omega;
+    double rA0rA, rA0rAold, tAtA, tAsA, zq;
+    double initRes, finalRes, trueRes;
+    double tol, relTol;
+    int nIter, maxIter, minIter, converged, singular, done;
+    int first;    // the next direction update starts a (re)start
+    int useBeta;  // direction update uses beta (0: p = z)
+    int early;    // BiCGStab converged on ||s|| inside the iteration
+    int flexible; // PCG: Polak-Ribiere beta
+    int status;   // 0 ok, otherwise an error code
+    int pad;
+};
+
+// Finalize operations run by the last block of a reducing kernel.
+enum Fin : int {
+    FIN_NONE = 0,
+    FIN_STORE,        // launch sums only (a later launch finalizes)
+    FIN_INIT_RES,     // initRes = finalRes = sqrt(sum0) + SMALL
+    FIN_PCG_WR,       // wArA (+ zq) -> singularity test, beta
+    FIN_PCG_ALPHA,    // wApA -> alpha
+    FIN_PCG_RES,      // finalRes, iteration count, convergence
+    FIN_BICG_INIT,    // initRes from sum0; sum1 = first rA0rA
+    FIN_BICG_ALPHA,   // rA0.AyA -> alpha
+    FIN_BICG_S,       // ||s|| -> early-exit test
+    FIN_BICG_OMEGA,   // tAtA, tA.sA -> omega
+    FIN_BICG_RES,     // ||r||, rA0.r -> iteration count, convergence
+    FIN_RES_ONLY,     // finalRes = sqrt(sum0) + SMALL (no iteration logic)
+    FIN_MG_RES,       // MGSolver: finalRes, iteration count, convergence
+    FIN_TRUE_RES,     // trueRes = sqrt(sum0) + SMALL
+};
+
+// One reduction site: per-block partials, per-launch sums, one ticket.
+struct RSpec {
+    double* blockPart = nullptr;  // >= gridDim.x * K
+    double* launchAcc = nullptr;  // >= nSlots * K
+    unsigned* ticket = nullptr;
+    int slot = 0;    // this launch's index into launchAcc
+    int nSlots = 1;  // launches to combine when finalizing
+    int fin = FIN_NONE;
+    KState* st = nullptr;
+};
+
+// Gate: skip the kernel when st->done (mask 1) or st->early (mask 2) is set.
+struct Gate {
+    const KState* st = nullptr;
+    int mask = 0;
+};
+
+// Device workspace for the reduction sites of one solver.
+struct RedPool {
+    DevArray<double> blockPart;  // nSites * maxBlocks * 4
+    DevArray<double> launchAcc;  // nSites * maxLaunch * 4
+    DevArray<unsigned> tickets;  // nSites
+    int nSites = 0, maxBlocks = 0, maxLaunch = 0;
+    void init(int sites, int blocks, int launches, cudaStream_t s);
+    RSpec site(int i, KState* st, int fin, int slot = 0, int nSlots = 1) const;
+};
+
+constexpr int kBlock = 256;
+constexpr int kRedK = 4;  // max values reduced together
+
+inline int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Launch context: stream and the grid cap (blocks) for grid-stride kernels.
+struct Exec {
+    cudaStream_t s = 0;
+    int maxBlocks = 1216;
+    int grid(long long n) const
+    {
+        int g = div_up(n, kBlock);
+        return g < 1 ? 1 : (g > maxBlocks ? maxBlocks : g);
+    }
+};
+
+int device_max_blocks();  // SMs * resident 256-thread blocks
+
+}  // namespace unapgpu
