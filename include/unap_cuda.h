@@ -153,6 +153,44 @@ int unap_cuda_krylov_solve(long int handle, int method, int precond, double tol,
                            int maxIter, int minIter, double* x, const double* b,
                            unap_cuda_stats* stats);
 
+/* ---- AMG-preconditioned PCG (no counterpart in the reference: its
+ * MGPrecond, src/preconditioners/MGPreconditioner/MGPreconditioner.cpp:35-42,
+ * is an empty stub).  The hierarchy is the reference's pairwise
+ * agglomeration (weights |upper|/||upper||, fortranInterface.cpp:383-395),
+ * continued until the coarsest level has at most nCoarsest cells; the
+ * V-cycle is x = 0, nPreSweeps forward Gauss-Seidel sweeps, restriction of
+ * b - A x, recursion, injection, nPostSweeps backward sweeps; the coarsest
+ * level is solved with a dense FP64 Cholesky-based inverse.  precision 1
+ * runs the whole V-cycle in FP32 inside the FP64 PCG (true residual, dot
+ * products, norms and the coarsest product stay FP64). */
+typedef struct {
+    int nCoarsest;   /* default 1000 */
+    int maxLevels;   /* default 50 */
+    int nPreSweeps;  /* default 2 */
+    int nPostSweeps; /* default 2 */
+    int precision;   /* 0 FP64 V-cycle, 1 FP32 V-cycle */
+    int flexible;    /* 1: Polak-Ribiere beta (default 1 when precision 1) */
+    double tol;      /* default 0 */
+    double relTol;   /* default 1e-10 */
+    int maxIter;     /* default 500 */
+    int minIter;     /* default 0 */
+} unap_cuda_amg_params;
+
+void unap_cuda_amg_default_params(unap_cuda_amg_params* p);
+/* builds the hierarchy of an existing matrix handle (the matrix must outlive
+ * the AMG handle) */
+int unap_cuda_amg_create(long int* amg, long int matrix, const unap_cuda_amg_params* p);
+/* nLevels including the finest; cells[k] for k < min(nLevels, maxOut) */
+int unap_cuda_amg_info(long int amg, int* nLevels, int* cells, int* wavefronts, int maxOut,
+                       double* setupSeconds, long long* deviceBytes);
+/* one V-cycle z = M^-1 r on device vectors in the caller's cell order */
+int unap_cuda_amg_vcycle(long int amg, const double* r, double* z);
+/* AMG-PCG on device vectors (x holds the initial guess) */
+int unap_cuda_amg_solve(long int amg, double* x, const double* b, unap_cuda_stats* stats);
+/* AMG-PCG on host vectors: copies b and x in, solves, copies x out */
+int unap_cuda_amg_solve_host(long int amg, double* x, const double* b, unap_cuda_stats* stats);
+int unap_cuda_amg_destroy(long int amg);
+
 int unap_cuda_device_synchronize(void);
 
 /* Kernel timings on the matrix's own stream with CUDA events (the GB300

@@ -79,7 +79,76 @@ SIGNATURES = {
     "unap_cuda_gauss_seidel": (_c_int, [_c_long, _vp, _vp, _c_int, _c_int]),
     "unap_cuda_krylov_solve": (_c_int, [_c_long, _c_int, _c_int, _c_dbl, _c_dbl, _c_int,
                                         _c_int, _vp, _vp, ctypes.POINTER(Stats)]),
+    "unap_cuda_amg_default_params": (None, [_vp]),
+    "unap_cuda_amg_create": (_c_int, [_lp, _c_long, _vp]),
+    "unap_cuda_amg_info": (_c_int, [_c_long, _ip, _vp, _vp, _c_int, _dp,
+                                    ctypes.POINTER(_c_ll)]),
+    "unap_cuda_amg_vcycle": (_c_int, [_c_long, _vp, _vp]),
+    "unap_cuda_amg_solve": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
+    "unap_cuda_amg_solve_host": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
+    "unap_cuda_amg_destroy": (_c_int, [_c_long]),
 }
+
+
+class AmgParams(ctypes.Structure):
+    _fields_ = [("nCoarsest", _c_int), ("maxLevels", _c_int), ("nPreSweeps", _c_int),
+                ("nPostSweeps", _c_int), ("precision", _c_int), ("flexible", _c_int),
+                ("tol", _c_dbl), ("relTol", _c_dbl), ("maxIter", _c_int), ("minIter", _c_int)]
+
+
+class DeviceAmg:
+    """AMG-preconditioned PCG on a DeviceMatrix (``unap_cuda_amg_*``)."""
+
+    def __init__(self, matrix: "DeviceMatrix", **kw):
+        lib = load()
+        self.params = AmgParams()
+        lib.unap_cuda_amg_default_params(ctypes.byref(self.params))
+        if kw.get("precision", 0) == 1 and "flexible" not in kw:
+            kw["flexible"] = 1
+        names = dict(n_coarsest="nCoarsest", max_levels="maxLevels", n_pre="nPreSweeps",
+                     n_post="nPostSweeps", precision="precision", flexible="flexible",
+                     tol="tol", rel_tol="relTol", max_iter="maxIter", min_iter="minIter")
+        for k, v in kw.items():
+            setattr(self.params, names[k], v)
+        h = _c_long(0)
+        check(lib.unap_cuda_amg_create(ctypes.byref(h), matrix.handle, ctypes.byref(self.params)))
+        self.handle = h.value
+        self.matrix = matrix
+
+    def info(self):
+        n = _c_int()
+        cells = np.zeros(64, np.int32)
+        waves = np.zeros(64, np.int32)
+        t = _c_dbl()
+        b = _c_ll()
+        check(load().unap_cuda_amg_info(self.handle, ctypes.byref(n), cells.ctypes.data,
+                                        waves.ctypes.data, 64, ctypes.byref(t), ctypes.byref(b)))
+        return dict(n_levels=n.value, cells=cells[:n.value].tolist(),
+                    wavefronts=waves[:n.value].tolist(), setup_s=t.value, device_bytes=b.value)
+
+    def vcycle(self, r, z):
+        check(load().unap_cuda_amg_vcycle(self.handle, _ptr(r), _ptr(z)))
+
+    def solve(self, x, b):
+        st = Stats()
+        check(load().unap_cuda_amg_solve(self.handle, _ptr(x), _ptr(b), ctypes.byref(st)))
+        return st.as_dict()
+
+    def solve_host(self, x, b):
+        st = Stats()
+        check(load().unap_cuda_amg_solve_host(self.handle, _ptr(x), _ptr(b), ctypes.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        if self.handle:
+            check(load().unap_cuda_amg_destroy(self.handle))
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def lib_path() -> str:

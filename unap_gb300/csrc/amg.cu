@@ -1,0 +1,223 @@
+// AMG hierarchy on the device and its V-cycle (see amg.hpp).
+#include <chrono>
+#include <climits>
+
+#include "amg.hpp"
+
+namespace unapgpu {
+
+namespace {
+
+template <class T>
+Rows<T> rowsT(const Level& L);
+template <>
+Rows<double> rowsT<double>(const Level& L)
+{
+    return rows64(L);
+}
+template <>
+Rows<float> rowsT<float>(const Level& L)
+{
+    return rows32(L);
+}
+
+struct Ext {
+    const double* r = nullptr;
+    double* z = nullptr;
+};
+thread_local Ext g_ext;
+
+}  // namespace
+
+AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
+{
+    auto t0 = std::chrono::steady_clock::now();
+    if (!A.host.symm) throw std::invalid_argument("AMG-PCG needs a symmetric matrix");
+    if (!A.L->sweepable)
+        throw std::invalid_argument("AMG smoothing needs oriented, owner-sorted faces");
+    cudaStream_t s = A.stream;
+    std::vector<double> w = mg_face_weights(A.host);
+    std::vector<CoarseHost> coarse =
+        agglomerate_levels(A.host, w, params.nCoarsest, params.maxLevels, 1);
+    const int L = (int)coarse.size();
+    lv.resize((size_t)L + 1);
+    lv[0].L = A.L.get();
+    lv[0].n = A.n();
+    for (int k = 1; k <= L; ++k) {
+        CoarseHost& c = coarse[(size_t)k - 1];
+        const Level& F = *lv[(size_t)k - 1].L;
+        const int nC = c.A.n;
+        // locality key of a coarse cell: first internal position of its cells
+        std::vector<int> key((size_t)nC, INT_MAX);
+        for (int i = 0; i < F.n; ++i) {
+            int C = c.restrictAddr[(size_t)i];
+            key[(size_t)C] = std::min(key[(size_t)C], F.iperm[(size_t)i]);
+        }
+        lv[(size_t)k].own = build_level(c.A, &key, k == L, s);
+        lv[(size_t)k].L = lv[(size_t)k].own.get();
+        lv[(size_t)k].n = nC;
+        const Level& Cl = *lv[(size_t)k].L;
+        // restriction: children of every coarse cell, ascending finer cell
+        // index (the summation order of restrictField), in internal indices
+        std::vector<int> refStart((size_t)nC + 1, 0);
+        for (int i = 0; i < F.n; ++i) refStart[(size_t)c.restrictAddr[(size_t)i] + 1]++;
+        for (int C = 0; C < nC; ++C) refStart[(size_t)C + 1] += refStart[(size_t)C];
+        std::vector<int> refChild((size_t)F.n);
+        {
+            std::vector<int> pos(refStart.begin(), refStart.end() - 1);
+            for (int i = 0; i < F.n; ++i) refChild[(size_t)pos[(size_t)c.restrictAddr[(size_t)i]]++] = i;
+        }
+        std::vector<int> cs((size_t)nC + 1, 0), ch((size_t)F.n);
+        for (int Ci = 0; Ci < nC; ++Ci) {
+            int C = Cl.perm[(size_t)Ci];
+            int len = refStart[(size_t)C + 1] - refStart[(size_t)C];
+            cs[(size_t)Ci + 1] = cs[(size_t)Ci] + len;
+            for (int j = 0; j < len; ++j)
+                ch[(size_t)(cs[(size_t)Ci] + j)] = F.iperm[(size_t)refChild[(size_t)(refStart[(size_t)C] + j)]];
+        }
+        std::vector<int> cmap((size_t)F.n);
+        for (int i = 0; i < F.n; ++i) cmap[(size_t)i] = Cl.iperm[(size_t)c.restrictAddr[(size_t)F.perm[(size_t)i]]];
+        lv[(size_t)k].childStart.upload(cs, s);
+        lv[(size_t)k].child.upload(ch, s);
+        lv[(size_t)k].cmap.upload(cmap, s);
+        UNAP_CK(cudaStreamSynchronize(s));
+    }
+    // coarsest: dense FP64 inverse (identity internal order when L >= 1)
+    const HostLdu& Ch = L ? coarse[(size_t)L - 1].A : A.host;
+    nc = Ch.n;
+    if (nc > 8192) throw std::invalid_argument("coarsest level too large for the dense solve");
+    {
+        const size_t N = (size_t)nc;
+        std::vector<double> dense(N * N, 0.0), inv;
+        for (int c = 0; c < nc; ++c) dense[(size_t)c * N + c] = Ch.diag[(size_t)c];
+        for (int f = 0; f < Ch.nf; ++f) {
+            dense[(size_t)Ch.l[(size_t)f] * N + Ch.u[(size_t)f]] += Ch.upper[(size_t)f];
+            dense[(size_t)Ch.u[(size_t)f] * N + Ch.l[(size_t)f]] += Ch.lowerPtr()[f];
+        }
+        if (!dense_spd_inverse(nc, dense, inv))
+            throw std::invalid_argument("coarsest matrix is not positive definite");
+        // column-major copy in the coarsest level's internal order (identity
+        // when L >= 1; the finest level's order when no coarse level exists)
+        const Level& CL = *lv[(size_t)L].L;
+        std::vector<double> cm(N * N);
+        for (int J = 0; J < nc; ++J)
+            for (int I = 0; I < nc; ++I)
+                cm[(size_t)J * N + I] = inv[(size_t)CL.perm[(size_t)I] * N + CL.perm[(size_t)J]];
+        Minv.upload(cm, s);
+    }
+    for (int k = 0; k <= L; ++k) {
+        size_t n = (size_t)lv[(size_t)k].n;
+        if (k > 0) {
+            lv[(size_t)k].x.alloc(n);
+            lv[(size_t)k].b.alloc(n);
+        }
+        lv[(size_t)k].r.alloc(n);
+        if (params.precision == 1) {
+            lv[(size_t)k].xf.alloc(n);
+            lv[(size_t)k].bf.alloc(n);
+            lv[(size_t)k].rf.alloc(n);
+            if (k < L) make_fp32(const_cast<Level&>(*lv[(size_t)k].L), s);
+        }
+    }
+    UNAP_CK(cudaStreamSynchronize(s));
+    setupSeconds =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+std::vector<int> AmgHierarchy::levelCells() const
+{
+    std::vector<int> v;
+    for (auto& l : lv) v.push_back(l.n);
+    return v;
+}
+
+std::vector<int> AmgHierarchy::levelWavefronts() const
+{
+    std::vector<int> v;
+    for (auto& l : lv) v.push_back(l.L->nWave);
+    return v;
+}
+
+size_t AmgHierarchy::deviceBytes() const
+{
+    size_t b = Minv.bytes();
+    for (size_t k = 0; k < lv.size(); ++k) {
+        const Lv& l = lv[k];
+        if (l.own) b += l.own->deviceBytes();
+        b += l.childStart.bytes() + l.child.bytes() + l.cmap.bytes() + l.x.bytes() + l.b.bytes() +
+             l.r.bytes() + l.xf.bytes() + l.bf.bytes() + l.rf.bytes();
+    }
+    return b;
+}
+
+template <>
+double* AmgHierarchy::X<double>(int k)
+{
+    return k == 0 ? g_ext.z : lv[(size_t)k].x.p;
+}
+template <>
+double* AmgHierarchy::B<double>(int k)
+{
+    return k == 0 ? const_cast<double*>(g_ext.r) : lv[(size_t)k].b.p;
+}
+template <>
+double* AmgHierarchy::R<double>(int k)
+{
+    return lv[(size_t)k].r.p;
+}
+template <>
+float* AmgHierarchy::X<float>(int k)
+{
+    return lv[(size_t)k].xf.p;
+}
+template <>
+float* AmgHierarchy::B<float>(int k)
+{
+    return lv[(size_t)k].bf.p;
+}
+template <>
+float* AmgHierarchy::R<float>(int k)
+{
+    return lv[(size_t)k].rf.p;
+}
+
+template <class T>
+void AmgHierarchy::vcycle_level(const Exec& ex, int k, Gate g)
+{
+    const int L = nLevels() - 1;
+    T* x = X<T>(k);
+    T* b = B<T>(k);
+    if (k == L) {
+        k_dense_apply<T>(ex, nc, Minv.p, b, x, g);
+        return;
+    }
+    const Level& Lk = *lv[(size_t)k].L;
+    Rows<T> Rk = rowsT<T>(Lk);
+    if (params.nPre > 0) {
+        for (int s = 0; s < params.nPre; ++s) gs_sweep<T>(ex, Lk, Rk, x, b, false, s == 0, g);
+    } else {
+        k_fill<T>(ex, Lk.n, x, T(0));
+    }
+    T* r = R<T>(k);
+    k_residual<T>(ex, Rk, x, b, r, RSpec{}, g);
+    const Lv& C = lv[(size_t)k + 1];
+    k_restrict<T>(ex, C.n, C.childStart.p, C.child.p, r, B<T>(k + 1), g);
+    vcycle_level<T>(ex, k + 1, g);
+    k_prolong_add<T>(ex, Lk.n, C.cmap.p, X<T>(k + 1), x, g);
+    for (int s = 0; s < params.nPost; ++s) gs_sweep<T>(ex, Lk, Rk, x, b, true, false, g);
+}
+
+void AmgHierarchy::vcycle(const Exec& ex, const double* r, double* z, Gate g)
+{
+    g_ext.r = r;
+    g_ext.z = z;
+    if (params.precision == 1) {
+        k_d2f(ex, lv[0].n, r, lv[0].bf.p);
+        vcycle_level<float>(ex, 0, g);
+        k_f2d(ex, lv[0].n, lv[0].xf.p, z);
+    } else {
+        vcycle_level<double>(ex, 0, g);
+    }
+}
+
+}  // namespace unapgpu

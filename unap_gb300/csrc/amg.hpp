@@ -1,0 +1,88 @@
+// Agglomeration AMG on the device: hierarchy, V-cycle, AMG-PCG.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "engine.hpp"
+
+namespace unapgpu {
+
+// One coarse level produced by the host agglomeration (reference numbering).
+struct CoarseHost {
+    HostLdu A;
+    std::vector<int> restrictAddr;  // finer cells -> this level's cells
+    std::vector<int> faceRestrict;  // finer faces -> coarse face, or -(cell+1)
+};
+
+std::vector<int> pairwise_pass(const HostLdu& A, const std::vector<double>& w, int& nCoarse);
+void coarse_addressing(const HostLdu& fine, const std::vector<int>& map, int nCoarse,
+                       CoarseHost& out);
+void coarse_coefficients(const HostLdu& fine, CoarseHost& c);
+// stopRule 0: the reference's rule (keep a level while it has >= nCoarsest
+// cells); stopRule 1: agglomerate until the coarsest has <= nCoarsest cells.
+std::vector<CoarseHost> agglomerate_levels(const HostLdu& fine, const std::vector<double>& weights,
+                                           int nCoarsest, int maxLevels, int stopRule);
+std::vector<double> mg_face_weights(const HostLdu& A);
+
+struct AmgParams {
+    int nCoarsest = 1000;
+    int maxLevels = 50;
+    int nPre = 2, nPost = 2;
+    int precision = 0;  // 0 FP64 V-cycle, 1 FP32 V-cycle (coarsest solve FP64)
+};
+
+// Device hierarchy for AMG as a fixed, symmetric PCG preconditioner:
+//   level k < L: x = 0; nPre forward GS sweeps; r = b - A x; b' = R r;
+//                e = V(k+1, b'); x += P e; nPost backward GS sweeps
+//   level L:     x = Minv b (dense FP64 inverse, rows summed in column order)
+// R sums the aggregate's cells in ascending cell order, P injects.
+class AmgHierarchy {
+public:
+    AmgHierarchy(Matrix& A, const AmgParams& p);
+    int nLevels() const { return (int)lv.size(); }
+    std::vector<int> levelCells() const;
+    std::vector<int> levelWavefronts() const;
+    // z = M^-1 r, internal order of the finest level
+    void vcycle(const Exec& ex, const double* r, double* z, Gate g);
+    AmgParams params;
+    double setupSeconds = 0;
+    size_t deviceBytes() const;
+
+    struct Lv {
+        const Level* L = nullptr;        // device structure (level 0: the matrix's)
+        std::unique_ptr<Level> own;
+        int n = 0;
+        DevArray<int> childStart, child;  // restriction into this level (k >= 1)
+        DevArray<int> cmap;               // prolongation from this level (k >= 1)
+        DevArray<double> x, b, r;
+        DevArray<float> xf, bf, rf;
+    };
+    std::vector<Lv> lv;
+    DevArray<double> Minv;  // coarsest dense inverse, column-major
+    int nc = 0;
+
+private:
+    Matrix& A;
+    template <class T>
+    void vcycle_level(const Exec& ex, int k, Gate g);
+    template <class T>
+    T* X(int k);
+    template <class T>
+    T* B(int k);
+    template <class T>
+    T* R(int k);
+};
+
+class AmgPrecond : public Precond {
+public:
+    explicit AmgPrecond(AmgHierarchy& h) : H(h) {}
+    void apply(const Exec& ex, const double* r, double* w, const RedPool*, int, KState*, int,
+               Gate g) override
+    {
+        H.vcycle(ex, r, w, g);
+    }
+    AmgHierarchy& H;
+};
+
+}  // namespace unapgpu

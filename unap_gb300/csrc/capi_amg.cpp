@@ -1,0 +1,178 @@
+// C ABI of the AMG-PCG solver (declared in include/unap_cuda.h).
+#include <cstdio>
+#include <memory>
+
+#include "amg.hpp"
+#include "capi_handles.hpp"
+#include "../../include/unap_cuda.h"
+
+using namespace unapgpu;
+
+namespace {
+
+struct AmgHandle {
+    static constexpr unsigned kMagic = 0x414d4731u;  // "AMG1"
+    unsigned magic = kMagic;
+    Matrix* A = nullptr;
+    unap_cuda_amg_params p{};
+    std::unique_ptr<AmgHierarchy> H;
+    std::unique_ptr<AmgPrecond> P;
+    std::unique_ptr<Krylov> K;
+    DevArray<double> dx, db;  // staging for host solves (reference order)
+    ~AmgHandle() { magic = 0; }
+};
+
+AmgHandle* amg_from(long int h)
+{
+    AmgHandle* a = reinterpret_cast<AmgHandle*>(h);
+    if (!a || a->magic != AmgHandle::kMagic) throw std::invalid_argument("invalid AMG handle");
+    return a;
+}
+
+template <class F>
+int guarded(F&& f)
+{
+    try {
+        f();
+        return UNAP_CUDA_OK;
+    } catch (const CudaError& e) {
+        set_last_error(e.what());
+        return UNAP_CUDA_ECUDA;
+    } catch (const std::invalid_argument& e) {
+        set_last_error(e.what());
+        return UNAP_CUDA_EINVAL;
+    } catch (const std::bad_alloc&) {
+        set_last_error("out of host memory");
+        return UNAP_CUDA_ENOMEM;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return UNAP_CUDA_EINTERNAL;
+    }
+}
+
+void put(const SolveStats& s, unap_cuda_stats* o)
+{
+    if (!o) return;
+    o->nIterations = s.nIter;
+    o->converged = s.converged;
+    o->singular = s.singular;
+    o->status = s.status;
+    o->initialResidual = s.initRes;
+    o->finalResidual = s.finalRes;
+    o->trueResidual = s.trueRes;
+    o->seconds = s.seconds;
+}
+
+}  // namespace
+
+extern "C" {
+
+void unap_cuda_amg_default_params(unap_cuda_amg_params* p)
+{
+    if (!p) return;
+    p->nCoarsest = 1000;
+    p->maxLevels = 50;
+    p->nPreSweeps = 2;
+    p->nPostSweeps = 2;
+    p->precision = 0;
+    p->flexible = 0;
+    p->tol = 0.0;
+    p->relTol = 1e-10;
+    p->maxIter = 500;
+    p->minIter = 0;
+}
+
+int unap_cuda_amg_create(long int* amg, long int matrix, const unap_cuda_amg_params* p)
+{
+    return guarded([&] {
+        if (!amg) throw std::invalid_argument("null handle pointer");
+        auto h = std::make_unique<AmgHandle>();
+        if (p)
+            h->p = *p;
+        else
+            unap_cuda_amg_default_params(&h->p);
+        if (h->p.precision != 0 && h->p.precision != 1)
+            throw std::invalid_argument("precision must be 0 (FP64) or 1 (FP32 V-cycle)");
+        h->A = &mat_from(matrix)->get();
+        AmgParams ap;
+        ap.nCoarsest = h->p.nCoarsest;
+        ap.maxLevels = h->p.maxLevels;
+        ap.nPre = h->p.nPreSweeps;
+        ap.nPost = h->p.nPostSweeps;
+        ap.precision = h->p.precision;
+        h->H = std::make_unique<AmgHierarchy>(*h->A, ap);
+        h->P = std::make_unique<AmgPrecond>(*h->H);
+        h->K = std::make_unique<Krylov>(*h->A, h->P.get(), Method::PCG);
+        h->K->tol = h->p.tol;
+        h->K->relTol = h->p.relTol;
+        h->K->maxIter = h->p.maxIter;
+        h->K->minIter = h->p.minIter;
+        h->K->flexible = h->p.flexible != 0;
+        h->K->trueResidualRestart = true;
+        *amg = reinterpret_cast<long int>(h.release());
+    });
+}
+
+int unap_cuda_amg_info(long int amg, int* nLevels, int* cells, int* wavefronts, int maxOut,
+                       double* setupSeconds, long long* deviceBytes)
+{
+    return guarded([&] {
+        AmgHandle* h = amg_from(amg);
+        std::vector<int> c = h->H->levelCells(), w = h->H->levelWavefronts();
+        if (nLevels) *nLevels = (int)c.size();
+        for (int k = 0; k < (int)c.size() && k < maxOut; ++k) {
+            if (cells) cells[k] = c[(size_t)k];
+            if (wavefronts) wavefronts[k] = w[(size_t)k];
+        }
+        if (setupSeconds) *setupSeconds = h->H->setupSeconds;
+        if (deviceBytes) *deviceBytes = (long long)h->H->deviceBytes();
+    });
+}
+
+int unap_cuda_amg_vcycle(long int amg, const double* r, double* z)
+{
+    return guarded([&] {
+        AmgHandle* h = amg_from(amg);
+        Matrix& A = *h->A;
+        Exec ex{A.stream, device_max_blocks()};
+        const int n = A.n();
+        DevArray<double> ri((size_t)n), zi((size_t)n);
+        k_to_internal<double>(ex, n, A.L->d_perm.p, r, ri.p);
+        h->H->vcycle(ex, ri.p, zi.p, Gate{});
+        k_to_reference<double>(ex, n, A.L->d_perm.p, zi.p, z);
+        UNAP_CK(cudaGetLastError());
+        UNAP_CK(cudaStreamSynchronize(A.stream));
+    });
+}
+
+int unap_cuda_amg_solve(long int amg, double* x, const double* b, unap_cuda_stats* stats)
+{
+    return guarded([&] {
+        AmgHandle* h = amg_from(amg);
+        put(h->K->solveDevice(x, b), stats);
+    });
+}
+
+int unap_cuda_amg_solve_host(long int amg, double* x, const double* b, unap_cuda_stats* stats)
+{
+    return guarded([&] {
+        AmgHandle* h = amg_from(amg);
+        Matrix& A = *h->A;
+        const size_t n = (size_t)A.n();
+        if (h->dx.n != n) h->dx.alloc(n);
+        if (h->db.n != n) h->db.alloc(n);
+        UNAP_CK(cudaMemcpyAsync(h->db.p, b, n * sizeof(double), cudaMemcpyHostToDevice, A.stream));
+        UNAP_CK(cudaMemcpyAsync(h->dx.p, x, n * sizeof(double), cudaMemcpyHostToDevice, A.stream));
+        SolveStats st = h->K->solveDevice(h->dx.p, h->db.p);
+        UNAP_CK(cudaMemcpyAsync(x, h->dx.p, n * sizeof(double), cudaMemcpyDeviceToHost, A.stream));
+        UNAP_CK(cudaStreamSynchronize(A.stream));
+        put(st, stats);
+    });
+}
+
+int unap_cuda_amg_destroy(long int amg)
+{
+    return guarded([&] { delete amg_from(amg); });
+}
+
+}  // extern "C"
