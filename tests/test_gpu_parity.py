@@ -94,24 +94,66 @@ def _solution_close(x, x_ref):
     return np.linalg.norm(x - x_ref) <= SOL_RTOL * max(np.linalg.norm(x_ref), 1e-300)
 
 
+def residual_space_close(orc, s, x, x_ref, rel_tol, r0):
+    """Two solutions that both meet ||b - A x|| <= relTol ||r0|| differ by at
+    most 2 relTol ||r0|| in residual space; that is the agreement a
+    tolerance-terminated solve can promise."""
+    d = orc.spmv(s, x - x_ref)
+    return np.linalg.norm(d) <= 2.2 * rel_tol * r0
+
+
+def iterations_match(it, it_ref, precond):
+    # unpreconditioned CG/BiCGStab on ill-conditioned systems amplifies the
+    # rounding of the dot products (summation order differs from the CPU's);
+    # preconditioned solves must match within one iteration
+    if precond == 0:
+        return abs(it - it_ref) <= max(1, int(0.03 * it_ref))
+    return abs(it - it_ref) <= 1
+
+
 @pytest.mark.parametrize("method", [0, 1])
 def test_krylov_parity(cuda, orc, method):
     torch = cuda
+    tol = 1e-8
     for s in systems():
         A = capi.DeviceMatrix(s)
         for t in (0, 1, 2, 3):
             if method == 0 and not s.symm:
                 continue  # CG on a nonsymmetric matrix diverges chaotically
             x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
-            st = A.krylov_solve(method, t, x, dev(torch, s.b), rel_tol=1e-8, max_iter=500)
+            st = A.krylov_solve(method, t, x, dev(torch, s.b), rel_tol=tol, max_iter=500)
             if method == 0:
-                x_ref, st_ref = orc.pcg(s, t, s.b, rel_tol=1e-8, max_iter=500)
+                x_ref, st_ref = orc.pcg(s, t, s.b, rel_tol=tol, max_iter=500)
             else:
-                x_ref, st_ref = orc.pbicgstab(s, t, s.b, rel_tol=1e-8, max_iter=500)
-            assert abs(st["nIterations"] - st_ref["n_iter"]) <= 1, (s.name, method, t, st, st_ref)
+                x_ref, st_ref = orc.pbicgstab(s, t, s.b, rel_tol=tol, max_iter=500)
+            assert iterations_match(st["nIterations"], st_ref["n_iter"], t), (
+                s.name, method, t, st, st_ref)
             assert st["converged"] == st_ref["converged"]
             assert np.isclose(st["initialResidual"], st_ref["init_res"], rtol=1e-12)
-            assert _solution_close(host(x), x_ref), (s.name, method, t)
+            if st["converged"]:
+                assert residual_space_close(orc, s, host(x), x_ref, tol,
+                                            st_ref["init_res"]), (s.name, method, t)
+        A.close()
+
+
+@pytest.mark.parametrize("method,precond", [(0, 2), (1, 3)])
+def test_solution_parity_tight(cuda, orc, method, precond):
+    """At relTol 1e-12 the GPU and oracle solutions agree within 1e-10
+    relative 2-norm (well-conditioned cases; the near-singular Neumann
+    Laplacian is left to the residual-space check above)."""
+    torch = cuda
+    cases = [W.laplace(14, 12, 10, seed=11, permute=True, rhs="normal", shift=0.5),
+             W.lognormal(12, seed=12, permute=True, sigma=1.0, shift=0.1)]
+    if method == 1:
+        cases.append(W.convdiff(12, 10, 9, seed=13, permute=True, pe=3.0))
+    for s in cases:
+        A = capi.DeviceMatrix(s)
+        x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+        st = A.krylov_solve(method, precond, x, dev(torch, s.b), rel_tol=1e-12, max_iter=1000)
+        fn = orc.pcg if method == 0 else orc.pbicgstab
+        x_ref, st_ref = fn(s, precond, s.b, rel_tol=1e-12, max_iter=1000)
+        assert abs(st["nIterations"] - st_ref["n_iter"]) <= 1, (s.name, st, st_ref)
+        assert _solution_close(host(x), x_ref), (s.name, method, precond)
         A.close()
 
 
@@ -135,4 +177,4 @@ def test_fortran_oneshot_matches_oracle(cuda, orc):
             x, it, res = fn(np.zeros(s.n), h, s.b, precond=t, rel_tol=1e-9)
             x_ref, st = ofn(s, t, s.b, rel_tol=1e-9)
             assert abs(it - st["n_iter"]) <= 1
-            assert _solution_close(x, x_ref)
+            assert residual_space_close(orc, s, x, x_ref, 1e-9, st["init_res"])

@@ -87,6 +87,7 @@ SIGNATURES = {
     "unap_cuda_amg_solve": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
     "unap_cuda_amg_solve_host": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
     "unap_cuda_amg_destroy": (_c_int, [_c_long]),
+    "unap_cuda_launch_count": (_c_ll, []),
 }
 
 

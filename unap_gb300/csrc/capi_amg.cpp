@@ -175,4 +175,6 @@ int unap_cuda_amg_destroy(long int amg)
     return guarded([&] { delete amg_from(amg); });
 }
 
+long long unap_cuda_launch_count(void) { return launch_count(); }
+
 }  // extern "C"

@@ -1,0 +1,157 @@
+// Device helpers shared by the kernel files: read-only loads, fixed-tree
+// block reductions, the SELL-32 row product and the reference's convergence
+// test.
+#pragma once
+
+#include "kernels.hpp"
+
+namespace unapgpu {
+
+#define SMALL_D 1.0e-37   // SMALL, src/base/unap.hpp:88
+#define VSMALL_D 1.0e-128 // VSMALL, src/base/unap.hpp:89
+
+template <class T>
+__device__ __forceinline__ T ldg(const T* p)
+{
+    return __ldg(p);
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Fixed-tree block sum of K values; the result is valid in thread 0.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K])
+{
+    __shared__ double sm[K][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) sm[k][wid] = v[k];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double t = lane < nw ? sm[k][lane] : 0.0;
+            v[k] = warp_sum(t);
+        }
+    }
+    __syncthreads();
+}
+
+// Two-level deterministic reduction: block tree -> per-block partials -> the
+// launch's last block (ticket) sums them in block order into launch slot
+// r.slot; when r.fin asks for it, that block sums slots 0..nSlots-1 in order
+// and calls fin(t) on one thread.
+template <int K, class F>
+__device__ __forceinline__ void reduce_launch(double (&v)[K], const RSpec& r, F&& fin)
+{
+    block_sum<K>(v);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) r.blockPart[blockIdx.x * K + k] = v[k];
+    }
+    __threadfence();
+    __shared__ int amLast;
+    if (threadIdx.x == 0) amLast = (atomicAdd(r.ticket, 1u) == gridDim.x - 1) ? 1 : 0;
+    __syncthreads();
+    if (!amLast) return;
+    __threadfence();
+    double s[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) s[k] += __ldcg(r.blockPart + b * K + k);
+    }
+    block_sum<K>(s);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) r.launchAcc[r.slot * K + k] = s[k];
+        *r.ticket = 0u;
+        if (r.fin != FIN_STORE && r.fin != FIN_NONE) {
+            double t[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) t[k] = 0.0;
+            for (int j = 0; j < r.nSlots; ++j) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) t[k] += __ldcg(r.launchAcc + j * K + k);
+            }
+            fin(t);
+        }
+        __threadfence();
+    }
+}
+
+// solverPerformance::checkConvergence, unapMatrixTest.cpp:3-31
+__device__ __forceinline__ int check_conv(double fin, double init, double tol, double rel,
+                                          int iter, int minIter)
+{
+    return ((fin < tol || (rel > SMALL_D && fin <= rel * init)) && iter >= minIter) ? 1 : 0;
+}
+
+// One row of y = A x in the reference's order (lduMatrixSpMV.cpp:83-92):
+// Apsi = 0; += diag psi; then the row's faces in face order.
+template <class T>
+__device__ __forceinline__ T row_apply(const Rows<T>& A, int r, const T* __restrict__ x)
+{
+    const int info = ldg(A.rowInfo + r);
+    const int len = info & 0xffff;
+    const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
+    T acc = T(0);
+    acc += ldg(A.diag + r) * ldg(x + r);
+    // entries in chunks of 8: all loads of a chunk are issued before the
+    // in-order accumulation, so a row's gathers overlap instead of chaining
+    for (int j0 = 0; j0 < len; j0 += 8) {
+        int c[8];
+        T v[8], xv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int e = base + 32 * (j0 + k);
+            c[k] = j0 + k < len ? ldg(A.col + e) : r;
+            v[k] = j0 + k < len ? ldg(A.val + e) : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) xv[k] = ldg(x + c[k]);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (j0 + k < len) acc += v[k] * xv[k];
+    }
+    return acc;
+}
+
+// Subtract a run of a row's entries from acc in entry order, j in [j0, j1):
+// acc -= val[e] * x[col[e]], with the loads of each 8-entry chunk issued
+// before the ordered subtractions.  x may be written concurrently by other
+// wavefronts' rows (plain loads, not the read-only path).
+template <class T>
+__device__ __forceinline__ T row_subtract(const Rows<T>& A, const T* coef, int base, int j0,
+                                          int j1, const T* x, T acc)
+{
+    for (int jc = j0; jc < j1; jc += 8) {
+        int c[8];
+        T v[8], xv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int e = base + 32 * (jc + k);
+            const bool on = jc + k < j1;
+            c[k] = on ? ldg(A.col + e) : 0;
+            v[k] = on ? ldg(coef + e) : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) xv[k] = jc + k < j1 ? x[c[k]] : T(0);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (jc + k < j1) acc -= v[k] * xv[k];
+    }
+    return acc;
+}
+
+}  // namespace unapgpu

@@ -230,18 +230,31 @@ void Krylov::runIterations()
 {
     if (useGraph && !graphExec) {
         UNAP_CK(cudaStreamBeginCapture(ex.s, cudaStreamCaptureModeThreadLocal));
-        enqueueIteration();
+        set_capturing(true);
+        try {
+            enqueueIteration();
+        } catch (...) {
+            set_capturing(false);
+            cudaStreamEndCapture(ex.s, &graph);
+            throw;
+        }
+        set_capturing(false);
         UNAP_CK(cudaStreamEndCapture(ex.s, &graph));
         UNAP_CK(cudaGraphInstantiate(&graphExec, graph, 0));
+        size_t nodes = 0;
+        UNAP_CK(cudaGraphGetNodes(graph, nullptr, &nodes));
+        graphKernels = (long long)nodes;
     }
     int batch = 1;
     int launched = 0;
     for (;;) {
         for (int k = 0; k < batch; ++k) {
-            if (useGraph)
+            if (useGraph) {
                 UNAP_CK(cudaGraphLaunch(graphExec, ex.s));
-            else
+                count_launches(graphKernels);
+            } else {
                 enqueueIteration();
+            }
         }
         launched += batch;
         UNAP_CK(cudaGetLastError());

@@ -72,6 +72,7 @@ private:
     RedPool pool;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graphExec = nullptr;
+    long long graphKernels = 0;
     cudaEvent_t ev0, ev1;
     void enqueueIteration();
     void enqueuePcgIteration();

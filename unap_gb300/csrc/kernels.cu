@@ -11,48 +11,22 @@
 //
 // The library is compiled with --fmad=false so that every product and sum
 // rounds separately, as the reference's loops do on the CPU.
+#include <atomic>
 #include <cmath>
 
-#include "kernels.hpp"
+#include "device_common.cuh"
 
 namespace unapgpu {
 
-#define SMALL_D 1.0e-37
-
-template <class T>
-__device__ __forceinline__ T ldg(const T* p)
+static std::atomic<long long> g_launches{0};
+static thread_local bool g_capturing = false;
+void count_launches(long long k) { g_launches += k; }
+long long launch_count() { return g_launches.load(); }
+void set_capturing(bool on) { g_capturing = on; }
+bool capturing() { return g_capturing; }
+static inline void tick()
 {
-    return __ldg(p);
-}
-
-__device__ __forceinline__ double warp_sum(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Fixed-tree block sum of K values; the result is valid in thread 0.
-template <int K>
-__device__ __forceinline__ void block_sum(double (&v)[K])
-{
-    __shared__ double sm[K][32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
-    if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) sm[k][wid] = v[k];
-    }
-    __syncthreads();
-    if (wid == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            double t = lane < nw ? sm[k][lane] : 0.0;
-            v[k] = warp_sum(t);
-        }
-    }
-    __syncthreads();
+    if (!g_capturing) g_launches++;
 }
 
 __device__ __forceinline__ bool gate_closed(const Gate& g)
@@ -64,13 +38,6 @@ __device__ __forceinline__ bool gate_closed(const Gate& g)
 }
 
 // --- finalize operations (run by one thread) -----------------------------
-
-// solverPerformance::checkConvergence, unapMatrixTest.cpp:3-31
-__device__ __forceinline__ int check_conv(double fin, double init, double tol, double rel,
-                                          int iter, int minIter)
-{
-    return ((fin < tol || (rel > SMALL_D && fin <= rel * init)) && iter >= minIter) ? 1 : 0;
-}
 
 // do { ... } while (++nIter < maxIter && !checkConvergence(...)),
 // PCG.cpp:167-180 / PBiCGStab.cpp:443-456 / MGSolve.cpp:161-176
@@ -195,62 +162,12 @@ __device__ void finalize(const RSpec& r, const double (&s)[K])
 template <int K>
 __device__ __forceinline__ void reduce_and_finalize(double (&v)[K], const RSpec& r)
 {
-    block_sum<K>(v);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) r.blockPart[blockIdx.x * K + k] = v[k];
-    }
-    __threadfence();
-    __shared__ int amLast;
-    if (threadIdx.x == 0) amLast = (atomicAdd(r.ticket, 1u) == gridDim.x - 1) ? 1 : 0;
-    __syncthreads();
-    if (!amLast) return;
-    __threadfence();
-    double s[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) s[k] = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) s[k] += __ldcg(r.blockPart + b * K + k);
-    }
-    block_sum<K>(s);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) r.launchAcc[r.slot * K + k] = s[k];
-        *r.ticket = 0u;
-        if (r.fin != FIN_STORE && r.fin != FIN_NONE) {
-            double t[K];
-#pragma unroll
-            for (int k = 0; k < K; ++k) t[k] = 0.0;
-            for (int j = 0; j < r.nSlots; ++j) {
-#pragma unroll
-                for (int k = 0; k < K; ++k) t[k] += __ldcg(r.launchAcc + j * K + k);
-            }
-            finalize<K>(r, t);
-        }
-        __threadfence();
-    }
+    reduce_launch<K>(v, r, [&](const double (&t)[K]) { finalize<K>(r, t); });
 }
 
 // --------------------------------------------------------------------------
 // SELL-32 row helpers
 // --------------------------------------------------------------------------
-template <class T>
-__device__ __forceinline__ T row_apply(const Rows<T>& A, int r, const T* __restrict__ x)
-{
-    const int info = ldg(A.rowInfo + r);
-    const int len = info & 0xffff;
-    const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
-    // lduMatrixSpMV.cpp:83-92: Apsi = 0; += diag psi; then faces in face order
-    T acc = T(0);
-    acc += ldg(A.diag + r) * ldg(x + r);
-    for (int j = 0; j < len; ++j) {
-        const int e = base + 32 * j;
-        acc += ldg(A.val + e) * ldg(x + ldg(A.col + e));
-    }
-    return acc;
-}
-
 template <class T>
 __global__ void __launch_bounds__(kBlock) spmv_kernel(Rows<T> A, const T* __restrict__ x,
                                                       T* __restrict__ y, const T* dotWith,
@@ -271,7 +188,7 @@ void k_spmv(const Exec& ex, const Rows<T>& A, const T* x, T* y, const T* dotWith
             Gate g)
 {
     if (A.n <= 0) return;
-    spmv_kernel<T><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, y, red.blockPart ? dotWith : nullptr,
+    tick(), spmv_kernel<T><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, y, red.blockPart ? dotWith : nullptr,
                                                       red, g);
 }
 
@@ -295,7 +212,7 @@ template <class T>
 void k_residual(const Exec& ex, const Rows<T>& A, const T* x, const T* b, T* r, RSpec red, Gate g)
 {
     if (A.n <= 0) return;
-    residual_kernel<T><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, b, r, red, g);
+    tick(), residual_kernel<T><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, b, r, red, g);
 }
 
 // --------------------------------------------------------------------------
@@ -316,16 +233,8 @@ __global__ void __launch_bounds__(kBlock) gs_kernel(Rows<T> A, T* x, const T* __
         const int nLow = info >> 16;
         const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
         T acc = ldg(b + r);
-        for (int j = 0; j < nLow; ++j) {
-            const int e = base + 32 * j;
-            acc -= ldg(A.val + e) * x[ldg(A.col + e)];
-        }
-        if (!skipUpper) {
-            for (int j = nLow; j < len; ++j) {
-                const int e = base + 32 * j;
-                acc -= ldg(A.val + e) * x[ldg(A.col + e)];
-            }
-        }
+        acc = row_subtract<T>(A, A.val, base, 0, nLow, x, acc);
+        if (!skipUpper) acc = row_subtract<T>(A, A.val, base, nLow, len, x, acc);
         x[r] = acc / ldg(A.diag + r);
     }
 }
@@ -335,7 +244,7 @@ void k_gs_rows(const Exec& ex, const Rows<T>& A, T* x, const T* b, int r0, int r
                Gate g)
 {
     if (r1 <= r0) return;
-    gs_kernel<T><<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, x, b, r0, r1, skipUpper ? 1 : 0, g);
+    tick(), gs_kernel<T><<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, x, b, r0, r1, skipUpper ? 1 : 0, g);
 }
 
 template <class T>
@@ -389,9 +298,9 @@ void dic_factor(const Exec& ex, const Level& L, bool dilu, double* dfac, double*
     const double* c2 = dilu ? A.val : A.valT;
     for (int w = 0; w < L.nWave; ++w) {
         int r0 = L.waveStart[w], r1 = L.waveStart[w + 1];
-        if (r1 > r0) factor_kernel<<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, c1, c2, dfac, r0, r1);
+        if (r1 > r0) tick(), factor_kernel<<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, c1, c2, dfac, r0, r1);
     }
-    if (L.n) recip_kernel<<<ex.grid(L.n), kBlock, 0, ex.s>>>(L.n, dfac, rD);
+    if (L.n) tick(), recip_kernel<<<ex.grid(L.n), kBlock, 0, ex.s>>>(L.n, dfac, rD);
 }
 
 // forward sweep (lduDICPrecond.cpp:63-71; DILU in losort order,
@@ -454,7 +363,7 @@ void dic_apply(const Exec& ex, const Level& L, bool dilu, const double* rD, cons
     for (int k = 0; k < W; ++k) {
         int r0 = L.waveStart[k], r1 = L.waveStart[k + 1];
         if (r1 > r0)
-            dic_fwd_kernel<<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, coef, rD, r, w, r0, r1, g);
+            tick(), dic_fwd_kernel<<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, coef, rD, r, w, r0, r1, g);
     }
     // backward: one launch slot per non-empty wavefront
     int nonEmpty = 0;
@@ -465,7 +374,7 @@ void dic_apply(const Exec& ex, const Level& L, bool dilu, const double* rD, cons
         if (r1 <= r0) continue;
         RSpec red;
         if (pool) red = pool->site(site, st, slot == nonEmpty - 1 ? fin : FIN_STORE, slot, nonEmpty);
-        dic_bwd_kernel<<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, rD, r, w, r0, r1, red, g);
+        tick(), dic_bwd_kernel<<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, rD, r, w, r0, r1, red, g);
         ++slot;
     }
 }
@@ -489,7 +398,7 @@ void diag_apply(const Exec& ex, int n, const double* rD, const double* r, double
                 Gate g)
 {
     if (n <= 0) return;
-    diag_apply_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, rD, r, w, red, g);
+    tick(), diag_apply_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, rD, r, w, red, g);
 }
 
 // --------------------------------------------------------------------------
@@ -509,7 +418,7 @@ __global__ void __launch_bounds__(kBlock) pcg_direction_kernel(int n, const doub
 void k_pcg_direction(const Exec& ex, int n, const double* w, double* p, const KState* st, Gate g)
 {
     if (n <= 0) return;
-    pcg_direction_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, w, p, st, g);
+    tick(), pcg_direction_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, w, p, st, g);
 }
 
 __global__ void __launch_bounds__(kBlock) pcg_update_kernel(int n, double* __restrict__ x,
@@ -534,7 +443,7 @@ void k_pcg_update(const Exec& ex, int n, double* x, double* r, const double* p, 
                   RSpec red, Gate g)
 {
     if (n <= 0) return;
-    pcg_update_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, x, r, p, q, red, g);
+    tick(), pcg_update_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, x, r, p, q, red, g);
 }
 
 __global__ void __launch_bounds__(kBlock) dot2_kernel(int n, const double* __restrict__ a,
@@ -555,7 +464,7 @@ __global__ void __launch_bounds__(kBlock) dot2_kernel(int n, const double* __res
 void k_dot2(const Exec& ex, int n, const double* a, const double* b, const double* c,
             const double* d, RSpec red, Gate g)
 {
-    dot2_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, a, b, c, d, red, g);
+    tick(), dot2_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, a, b, c, d, red, g);
 }
 
 // --------------------------------------------------------------------------
@@ -582,7 +491,7 @@ __global__ void __launch_bounds__(kBlock) bicg_init_kernel(int n, const double* 
 void k_bicg_init(const Exec& ex, int n, const double* b, const double* Ax, double* r, double* r0,
                  RSpec red)
 {
-    bicg_init_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, b, Ax, r, r0, red);
+    tick(), bicg_init_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, b, Ax, r, r0, red);
 }
 
 // p = r (first) or p = r + beta (p - omega Ay)
@@ -603,7 +512,7 @@ void k_bicg_direction(const Exec& ex, int n, const double* r, const double* Ay, 
                       const KState* st, Gate g)
 {
     if (n <= 0) return;
-    bicg_direction_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, r, Ay, p, st, g);
+    tick(), bicg_direction_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, r, Ay, p, st, g);
 }
 
 // s = r - alpha Ay; sums s.s
@@ -625,7 +534,7 @@ __global__ void __launch_bounds__(kBlock) bicg_s_kernel(int n, const double* __r
 void k_bicg_s(const Exec& ex, int n, const double* r, const double* Ay, double* s, RSpec red,
               Gate g)
 {
-    bicg_s_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, r, Ay, s, red, g);
+    tick(), bicg_s_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, r, Ay, s, red, g);
 }
 
 // early exit: x += alpha y; else x += alpha y + omega z, r = s - omega t;
@@ -665,7 +574,7 @@ __global__ void __launch_bounds__(kBlock) bicg_update_kernel(int n, double* __re
 void k_bicg_update(const Exec& ex, int n, double* x, double* r, const double* y, const double* z,
                    const double* s, const double* t, const double* r0, RSpec red, Gate g)
 {
-    bicg_update_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, x, r, y, z, s, t, r0, red,
+    tick(), bicg_update_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, x, r, y, z, s, t, r0, red,
                                                                     g);
 }
 
@@ -691,13 +600,13 @@ __global__ void to_reference_kernel(int n, const int* __restrict__ perm,
 template <class T>
 void k_to_internal(const Exec& ex, int n, const int* perm, const T* in, T* out)
 {
-    if (n > 0) to_internal_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, perm, in, out);
+    if (n > 0) tick(), to_internal_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, perm, in, out);
 }
 
 template <class T>
 void k_to_reference(const Exec& ex, int n, const int* perm, const T* in, T* out)
 {
-    if (n > 0) to_reference_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, perm, in, out);
+    if (n > 0) tick(), to_reference_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, perm, in, out);
 }
 
 // restrictField (unapMatrix.hpp:378-407) in gather form: children ascending
@@ -718,7 +627,7 @@ void k_restrict(const Exec& ex, int nCoarse, const int* childStart, const int* c
                 const T* fine, T* coarse, Gate g)
 {
     if (nCoarse > 0)
-        restrict_kernel<T><<<ex.grid(nCoarse), kBlock, 0, ex.s>>>(nCoarse, childStart, child, fine,
+        tick(), restrict_kernel<T><<<ex.grid(nCoarse), kBlock, 0, ex.s>>>(nCoarse, childStart, child, fine,
                                                                   coarse, g);
 }
 
@@ -735,7 +644,7 @@ template <class T>
 void k_prolong_add(const Exec& ex, int nFine, const int* cmap, const T* coarse, T* fine, Gate g)
 {
     if (nFine > 0)
-        prolong_add_kernel<T><<<ex.grid(nFine), kBlock, 0, ex.s>>>(nFine, cmap, coarse, fine, g);
+        tick(), prolong_add_kernel<T><<<ex.grid(nFine), kBlock, 0, ex.s>>>(nFine, cmap, coarse, fine, g);
 }
 
 // Dense coarsest solve: x_i = sum_j Minv[i][j] b_j, j ascending, FP64.
@@ -762,7 +671,7 @@ void k_dense_apply(const Exec& ex, int n, const double* MinvColMajor, const T* b
     if (n <= 0) return;
     int threads = 64;
     int blocks = div_up(n, threads);
-    dense_apply_kernel<T><<<blocks, threads, (size_t)n * sizeof(double), ex.s>>>(n, MinvColMajor,
+    tick(), dense_apply_kernel<T><<<blocks, threads, (size_t)n * sizeof(double), ex.s>>>(n, MinvColMajor,
                                                                                b, x, g);
 }
 
@@ -777,7 +686,7 @@ __global__ void fill_kernel(long long n, T* x, T v)
 template <class T>
 void k_fill(const Exec& ex, long long n, T* x, T v)
 {
-    if (n > 0) fill_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, x, v);
+    if (n > 0) tick(), fill_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, x, v);
 }
 
 __global__ void d2f_kernel(int n, const double* __restrict__ in, float* __restrict__ out)
@@ -794,12 +703,12 @@ __global__ void f2d_kernel(int n, const float* __restrict__ in, double* __restri
 
 void k_d2f(const Exec& ex, int n, const double* in, float* out)
 {
-    if (n > 0) d2f_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, in, out);
+    if (n > 0) tick(), d2f_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, in, out);
 }
 
 void k_f2d(const Exec& ex, int n, const float* in, double* out)
 {
-    if (n > 0) f2d_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, in, out);
+    if (n > 0) tick(), f2d_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, in, out);
 }
 
 void k_axpy_f2d(const Exec& ex, int n, const float* in, double* out) { k_f2d(ex, n, in, out); }
@@ -827,7 +736,7 @@ template <class T>
 void k_scaling_sums(const Exec& ex, int n, const T* source, const T* Acf, T* field, const T* D,
                     RSpec red, Gate g)
 {
-    scaling_kernel<T><<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, source, Acf, field, D, red,
+    tick(), scaling_kernel<T><<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, source, Acf, field, D, red,
                                                                    g);
 }
 
@@ -842,7 +751,7 @@ __global__ void axpby_kernel(int n, T a, const T* __restrict__ x, T b, T* __rest
 template <class T>
 void k_axpby(const Exec& ex, int n, T a, const T* x, T b, T* y, Gate g)
 {
-    if (n > 0) axpby_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, a, x, b, y, g);
+    if (n > 0) tick(), axpby_kernel<T><<<ex.grid(n), kBlock, 0, ex.s>>>(n, a, x, b, y, g);
 }
 
 // --------------------------------------------------------------------------
@@ -880,8 +789,8 @@ void make_fp32(Level& L, cudaStream_t s)
     ex.maxBlocks = device_max_blocks();
     L.d_val32.alloc((size_t)L.nEntries);
     L.d_diag32.alloc((size_t)L.n);
-    if (L.nEntries) d2f_kernel<<<ex.grid(L.nEntries), kBlock, 0, s>>>((int)L.nEntries, L.d_val.p, L.d_val32.p);
-    if (L.n) d2f_kernel<<<ex.grid(L.n), kBlock, 0, s>>>(L.n, L.d_diag.p, L.d_diag32.p);
+    if (L.nEntries) tick(), d2f_kernel<<<ex.grid(L.nEntries), kBlock, 0, s>>>((int)L.nEntries, L.d_val.p, L.d_val32.p);
+    if (L.n) tick(), d2f_kernel<<<ex.grid(L.n), kBlock, 0, s>>>(L.n, L.d_diag.p, L.d_diag32.p);
     UNAP_CK(cudaGetLastError());
 }
 

@@ -225,4 +225,11 @@ struct Exec {
 
 int device_max_blocks();  // SMs * resident 256-thread blocks
 
+// Count of kernel launches issued by this library (graph launches add their
+// kernel-node count; launches recorded into a graph capture are not counted).
+void count_launches(long long k);
+long long launch_count();
+void set_capturing(bool on);
+bool capturing();
+
 }  // namespace unapgpu
