@@ -75,7 +75,35 @@ void pbicgstabsolversolve_(double* x, long int* APtrPtr, double* b, int* nCells,
                            double* tol, double* relTol, int* maxIter, int* minIter,
                            int* num_iterations, double* final_res_norm);
 
-/* Handle API, fortranInterface.hpp:173-331 / fortranInterface.cpp:537-1102 */
+/* fortranInterface.h:87-102 / fortranInterface.cpp:349-464.  aggl 1 weights
+ * |upper|/||upper||, 2 faceAreaPtr; smoother 1 GS, 2 Cheby; the reference's
+ * MGSolver defaults with nPreSweeps 0.  Deletes *APtrPtr. */
+void mgsolversolve_(double* x, long int* APtrPtr, double* b, int* nCells, int* aggl,
+                    int* smoother, double* tol, double* relTol, int* maxIter, int* minIter,
+                    int* num_iterations, double* final_res_norm, double* faceAreaPtr);
+
+/* Handle API, fortranInterface.hpp:173-331 / fortranInterface.cpp:537-1102.
+ * contruct_solver_mg__ builds the hierarchy at once (maxLevels, coarsest
+ * threshold as given); *AgglPtr receives a value identifying it (the
+ * hierarchy is owned by the MG handle).  sw_solve_mg__ resets the Chebyshev
+ * eigenvalue estimates (initSmoothers) before every solve, as the
+ * reference does; the hierarchy is rebuilt when the matrix coefficients
+ * changed since it was made. */
+void contruct_solver_mg__(long int* mgPtrPtr, long int* APtrPtr, long int* AgglPtr,
+                          const double* weightsPtr, const int* smootherTypePtr,
+                          const int* maxLevelsPtr, const int* nCellsCoarsestPtr);
+void sw_solver_mg_set_maxiter__(long int* solverPtrPtr, const int* maxIterPtr);
+void sw_solver_mg_set_miniter__(long int* solverPtrPtr, const int* minIterPtr);
+void sw_solver_mg_set_tol__(long int* solverPtrPtr, const double* tolPtr);
+void sw_solver_mg_set_reltol__(long int* solverPtrPtr, const double* reltolPtr);
+void sw_solver_mg_set_npresweeps__(long int* solverPtrPtr, const int* numPtr);
+void sw_solver_mg_set_npostsweeps__(long int* solverPtrPtr, const int* numPtr);
+void sw_solver_mg_set_nfinestsweeps__(long int* solverPtrPtr, const int* numPtr);
+void sw_solve_mg__(long int* mgPtrPtr, long int* APtrPtr, double* xPtr, double* bPtr,
+                   double* res_normPtr);
+void sw_solver_destroy_mg__(long int* solverPtrPtr);
+
+/* Handle API (PBiCGStab and matrices) */
 void contruct_sw_matrix__(long int* APtrPtr, const int* nCellsPtr, const int* rowsPtr,
                           const int* colsPtr, const int* sizePtr);
 void contruct_sw_matrix_interfaces__(long int* APtrPtr, const int* nNeiProcsPtr,
@@ -191,6 +219,17 @@ int unap_cuda_amg_solve(long int amg, double* x, const double* b, unap_cuda_stat
 int unap_cuda_amg_solve_host(long int amg, double* x, const double* b, unap_cuda_stats* stats);
 int unap_cuda_amg_destroy(long int amg);
 
+/* ---- MGSolver on device vectors (MGSolve.cpp:17-187).  weights NULL means
+ * |upper|/||upper||; negative nCoarsest/maxLevels/nPre/nPost/nFinest keep the
+ * reference defaults (50, 50, 0, 2, 2); scaleCorr -1 means "if symmetric". */
+int unap_cuda_mg_create(long int* mg, long int matrix, const double* weights, int smoother,
+                        int nCoarsest, int maxLevels, int nPre, int nPost, int nFinest,
+                        int scaleCorr, double tol, double relTol, int maxIter, int minIter);
+/* number of coarse levels; cells[k] for k <= nCoarseLevels (k = 0 finest) */
+int unap_cuda_mg_levels(long int mg, int* nCoarseLevels, int* cells, int maxOut);
+int unap_cuda_mg_solve(long int mg, double* x, const double* b, unap_cuda_stats* stats);
+int unap_cuda_mg_destroy(long int mg);
+
 int unap_cuda_device_synchronize(void);
 
 /* Kernel timings on the matrix's own stream with CUDA events (the GB300
@@ -204,6 +243,20 @@ int unap_cuda_profile_kernels(long int handle, int reps, double* ms);
 /* Kernel launches issued by this library since it was loaded (a CUDA-graph
  * launch counts its kernel nodes). */
 long long unap_cuda_launch_count(void);
+
+/* Executor of PCG solves created after the call: 1 (default) runs the whole
+ * solve as one persistent cooperative launch that executes a compiled step
+ * program; 0 launches one kernel per step, one iteration captured as a CUDA
+ * graph.  Both give the same iterates up to dot-product summation order.
+ * Returns the previous setting. */
+int unap_cuda_set_executor(int persistent);
+
+/* Failure-detection self-test of the persistent executor's bounded waits:
+ * one CTA sleeps (bounded) past a deliberately tiny barrier-wait bound, the
+ * other CTAs give up, the launch ends and reports the timeout
+ * (*timedOut = 1); a second launch with the normal bound then completes
+ * (*recovered = 1).  Nothing faults and nothing waits without a bound. */
+int unap_cuda_selftest_barrier_timeout(int* timedOut, int* recovered);
 
 #ifdef __cplusplus
 }

@@ -27,6 +27,16 @@ def ref():
     return Oracle("ref")
 
 
+@pytest.fixture(params=["persistent", "graph"])
+def executor(request, cuda):
+    """Runs a test once with the persistent step executor and once with
+    per-step kernel launches captured in a CUDA graph."""
+    from unap_gb300 import capi
+    old = capi.set_executor(request.param == "persistent")
+    yield request.param
+    capi.set_executor(old)
+
+
 @pytest.fixture(scope="session")
 def cuda():
     """torch with a CUDA device, and the product library loaded."""

@@ -47,7 +47,7 @@ def test_hierarchy_and_vcycle_bit_exact(cuda, orc, precision):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-def test_amg_pcg_parity(cuda, orc, precision):
+def test_amg_pcg_parity(cuda, orc, precision, executor):
     torch = cuda
     for s in spd_systems():
         A = capi.DeviceMatrix(s)

@@ -112,7 +112,7 @@ def iterations_match(it, it_ref, precond):
 
 
 @pytest.mark.parametrize("method", [0, 1])
-def test_krylov_parity(cuda, orc, method):
+def test_krylov_parity(cuda, orc, method, executor):
     torch = cuda
     tol = 1e-8
     for s in systems():

@@ -88,7 +88,68 @@ SIGNATURES = {
     "unap_cuda_amg_solve_host": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
     "unap_cuda_amg_destroy": (_c_int, [_c_long]),
     "unap_cuda_launch_count": (_c_ll, []),
+    "unap_cuda_set_executor": (_c_int, [_c_int]),
+    "unap_cuda_selftest_barrier_timeout": (_c_int, [_ip, _ip]),
+    "mgsolversolve_": (None, [_dp, _lp, _dp, _ip, _ip, _ip, _dp, _dp, _ip, _ip, _ip, _dp, _dp]),
+    "contruct_solver_mg__": (None, [_lp, _lp, _lp, _dp, _ip, _ip, _ip]),
+    "sw_solver_mg_set_maxiter__": (None, [_lp, _ip]),
+    "sw_solver_mg_set_miniter__": (None, [_lp, _ip]),
+    "sw_solver_mg_set_tol__": (None, [_lp, _dp]),
+    "sw_solver_mg_set_reltol__": (None, [_lp, _dp]),
+    "sw_solver_mg_set_npresweeps__": (None, [_lp, _ip]),
+    "sw_solver_mg_set_npostsweeps__": (None, [_lp, _ip]),
+    "sw_solver_mg_set_nfinestsweeps__": (None, [_lp, _ip]),
+    "sw_solve_mg__": (None, [_lp, _lp, _dp, _dp, _dp]),
+    "sw_solver_destroy_mg__": (None, [_lp]),
+    "unap_cuda_mg_create": (_c_int, [_lp, _c_long, _vp, _c_int, _c_int, _c_int, _c_int, _c_int,
+                                     _c_int, _c_int, _c_dbl, _c_dbl, _c_int, _c_int]),
+    "unap_cuda_mg_levels": (_c_int, [_c_long, _ip, _vp, _c_int]),
+    "unap_cuda_mg_solve": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
+    "unap_cuda_mg_destroy": (_c_int, [_c_long]),
 }
+
+
+class DeviceMG:
+    """The reference's MGSolver on a DeviceMatrix (``unap_cuda_mg_*``)."""
+
+    def __init__(self, matrix, weights=None, smoother=1, n_coarsest=-1, max_levels=-1,
+                 n_pre=-1, n_post=-1, n_finest=-1, scale_corr=-1, tol=0.0, rel_tol=1e-6,
+                 max_iter=1000, min_iter=0):
+        lib = load()
+        self._w = None if weights is None else _f64(weights)
+        h = _c_long(0)
+        check(lib.unap_cuda_mg_create(ctypes.byref(h), matrix.handle,
+                                      None if self._w is None else self._w.ctypes.data,
+                                      smoother, n_coarsest, max_levels, n_pre, n_post, n_finest,
+                                      scale_corr, tol, rel_tol, max_iter, min_iter))
+        self.handle = h.value
+
+    def levels(self):
+        n = _c_int()
+        cells = np.zeros(64, np.int32)
+        check(load().unap_cuda_mg_levels(self.handle, ctypes.byref(n), cells.ctypes.data, 64))
+        return cells[:n.value + 1].tolist()
+
+    def solve(self, x, b):
+        st = Stats()
+        check(load().unap_cuda_mg_solve(self.handle, _ptr(x), _ptr(b), ctypes.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        if self.handle:
+            check(load().unap_cuda_mg_destroy(self.handle))
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def set_executor(persistent: bool) -> bool:
+    """Executor of PCG solves created afterwards; returns the previous one."""
+    return bool(load().unap_cuda_set_executor(1 if persistent else 0))
 
 
 class AmgParams(ctypes.Structure):

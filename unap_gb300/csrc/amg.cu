@@ -1,6 +1,7 @@
 // AMG hierarchy on the device and its V-cycle (see amg.hpp).
 #include <chrono>
 #include <climits>
+#include <type_traits>
 
 #include "amg.hpp"
 
@@ -205,6 +206,122 @@ void AmgHierarchy::vcycle_level(const Exec& ex, int k, Gate g)
     vcycle_level<T>(ex, k + 1, g);
     k_prolong_add<T>(ex, Lk.n, C.cmap.p, X<T>(k + 1), x, g);
     for (int s = 0; s < params.nPost; ++s) gs_sweep<T>(ex, Lk, Rk, x, b, true, false, g);
+}
+
+template <class T>
+void AmgHierarchy::append_level(std::vector<Step>& out, int k, int tableBase)
+{
+    const int L = nLevels() - 1;
+    const int prec = std::is_same<T, float>::value ? 1 : 0;
+    const int lvl = k == 0 ? 0 : tableBase + k - 1;
+    T* x = X<T>(k);
+    T* b = B<T>(k);
+    auto step = [&](int op, bool single) {
+        Step s;
+        s.op = op;
+        s.prec = prec;
+        s.single = single ? 1 : 0;
+        s.lvl = lvl;
+        return s;
+    };
+    if (k == L) {
+        Step s = step(ST_DENSE, true);
+        s.r1 = nc;
+        s.e = Minv.p;
+        s.a = b;
+        s.c = x;
+        out.push_back(s);
+        return;
+    }
+    const Level& Lk = *lv[(size_t)k].L;
+    const bool single = mega_single_level(Lk.n);
+    if (params.nPre > 0) {
+        for (int sw = 0; sw < params.nPre; ++sw)
+            for (int w = 0; w < Lk.nWave; ++w) {
+                Step s = step(ST_GS, single);
+                s.r0 = Lk.waveStart[(size_t)w];
+                s.r1 = Lk.waveStart[(size_t)w + 1];
+                s.f0 = sw == 0 ? 1 : 0;  // first sweep from x = 0: upper side is zero
+                s.b = b;
+                s.c = x;
+                out.push_back(s);
+            }
+    } else {
+        Step s = step(ST_FILL0, single);
+        s.r1 = Lk.n;
+        s.c = x;
+        out.push_back(s);
+    }
+    {
+        Step s = step(ST_RESID, single);
+        s.a = x;
+        s.b = b;
+        s.c = R<T>(k);
+        out.push_back(s);
+    }
+    const Lv& C = lv[(size_t)k + 1];
+    {
+        Step s = step(ST_RESTRICT, single);
+        s.r1 = C.n;
+        s.i0 = C.childStart.p;
+        s.i1 = C.child.p;
+        s.a = R<T>(k);
+        s.c = B<T>(k + 1);
+        out.push_back(s);
+    }
+    append_level<T>(out, k + 1, tableBase);
+    {
+        Step s = step(ST_PROLONG_ADD, single);
+        s.r1 = Lk.n;
+        s.i0 = C.cmap.p;
+        s.a = X<T>(k + 1);
+        s.c = x;
+        out.push_back(s);
+    }
+    for (int sw = 0; sw < params.nPost; ++sw)
+        for (int w = Lk.nWave - 1; w >= 0; --w) {
+            Step s = step(ST_GS, single);
+            s.r0 = Lk.waveStart[(size_t)w];
+            s.r1 = Lk.waveStart[(size_t)w + 1];
+            s.b = b;
+            s.c = x;
+            out.push_back(s);
+        }
+}
+
+void AmgHierarchy::appendVcycle(std::vector<Step>& out, std::vector<LevelRows>& table,
+                                const double* r, double* z)
+{
+    g_ext.r = r;
+    g_ext.z = z;
+    const int tableBase = (int)table.size();
+    for (int k = 1; k < nLevels(); ++k) {
+        LevelRows e;
+        e.r64 = rows64(*lv[(size_t)k].L);
+        if (lv[(size_t)k].L->d_val32.p) e.r32 = rows32(*lv[(size_t)k].L);
+        table.push_back(e);
+    }
+    const int n0 = lv[0].n;
+    if (params.precision == 1) {
+        table[0].r32 = rows32(*lv[0].L);
+        Step s;
+        s.op = ST_D2F;
+        s.single = mega_single_level(n0);
+        s.r1 = n0;
+        s.a = r;
+        s.c = lv[0].bf.p;
+        out.push_back(s);
+        append_level<float>(out, 0, tableBase);
+        Step t;
+        t.op = ST_F2D;
+        t.single = s.single;
+        t.r1 = n0;
+        t.a = lv[0].xf.p;
+        t.c = z;
+        out.push_back(t);
+    } else {
+        append_level<double>(out, 0, tableBase);
+    }
 }
 
 void AmgHierarchy::vcycle(const Exec& ex, const double* r, double* z, Gate g)

@@ -45,6 +45,9 @@ public:
     std::vector<int> levelWavefronts() const;
     // z = M^-1 r, internal order of the finest level
     void vcycle(const Exec& ex, const double* r, double* z, Gate g);
+    // the same V-cycle as a step program (mega.hpp); lv[0] is the finest
+    void appendVcycle(std::vector<Step>& out, std::vector<LevelRows>& lv, const double* r,
+                      double* z);
     AmgParams params;
     double setupSeconds = 0;
     size_t deviceBytes() const;
@@ -67,6 +70,8 @@ private:
     template <class T>
     void vcycle_level(const Exec& ex, int k, Gate g);
     template <class T>
+    void append_level(std::vector<Step>& out, int k, int tableBase);
+    template <class T>
     T* X(int k);
     template <class T>
     T* B(int k);
@@ -81,6 +86,13 @@ public:
                Gate g) override
     {
         H.vcycle(ex, r, w, g);
+    }
+    bool appendSteps(std::vector<Step>& out, std::vector<LevelRows>& lv, const double* r,
+                     double* w, int, bool* dotFused) override
+    {
+        H.appendVcycle(out, lv, r, w);
+        *dotFused = false;
+        return true;
     }
     AmgHierarchy& H;
 };

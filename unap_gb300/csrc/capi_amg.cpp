@@ -177,4 +177,32 @@ int unap_cuda_amg_destroy(long int amg)
 
 long long unap_cuda_launch_count(void) { return launch_count(); }
 
+int unap_cuda_set_executor(int persistent) { return set_default_executor(persistent); }
+
+int unap_cuda_selftest_barrier_timeout(int* timedOut, int* recovered)
+{
+    return guarded([&] {
+        cudaStream_t s;
+        UNAP_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        // CTA 0 sleeps 20 ms inside a single-CTA segment while the other CTAs
+        // wait at the following grid barrier with a ~64 us bound
+        std::vector<Step> steps(1);
+        steps[0].op = ST_SLEEP;
+        steps[0].single = 1;
+        steps[0].f0 = 20000;
+        std::vector<LevelRows> lv(1);
+        MegaRunner R;
+        R.setProgram(steps, 1, lv, 1, s);
+        DevArray<KState> st(1);
+        st.zero(s);
+        bool ok = R.run(st.p, 1, s, false, 2000);
+        if (timedOut) *timedOut = ok ? 0 : 1;
+        // the context stays usable: the same program with the default bound
+        bool ok2 = R.run(st.p, 1, s, false, 0);
+        UNAP_CK(cudaStreamSynchronize(s));
+        UNAP_CK(cudaStreamDestroy(s));
+        if (recovered) *recovered = ok2 ? 1 : 0;
+    });
+}
+
 }  // extern "C"

@@ -154,4 +154,124 @@ __device__ __forceinline__ T row_subtract(const Rows<T>& A, const T* coef, int b
     return acc;
 }
 
+// --- finalize operations (run by one thread) -----------------------------
+
+// do { ... } while (++nIter < maxIter && !checkConvergence(...)),
+// PCG.cpp:167-180 / PBiCGStab.cpp:443-456 / MGSolve.cpp:161-176
+__device__ __forceinline__ void iteration_end(KState* st)
+{
+    st->nIter++;
+    if (!(st->nIter < st->maxIter)) {
+        st->done = 1;
+        return;
+    }
+    st->converged = check_conv(st->finalRes, st->initRes, st->tol, st->relTol, st->nIter,
+                               st->minIter);
+    if (st->converged) st->done = 1;
+}
+
+// rA0rA update at the top of a PBiCGStab iteration (PBiCGStab.cpp:155-243)
+__device__ __forceinline__ void bicg_rr(KState* st, double rr)
+{
+    st->rA0rAold = st->rA0rA;
+    st->rA0rA = rr;
+    if (!(fabs(st->rA0rA) > SMALL_D)) {
+        st->singular = 1;
+        st->done = 1;
+        return;
+    }
+    if (st->first) {
+        st->useBeta = 0;
+        st->first = 0;
+    } else {
+        st->useBeta = 1;
+        st->beta = (st->rA0rA / st->rA0rAold) * (st->alpha / st->omega);
+    }
+}
+
+// Solver-state update run once per reduction site with the site sums s[0..K).
+__device__ __forceinline__ void apply_fin(KState* st, int fin, const double* s, int K)
+{
+    switch (fin) {
+    case FIN_INIT_RES:
+        st->initRes = sqrt(s[0]) + SMALL_D;
+        st->finalRes = st->initRes;
+        break;
+    case FIN_RES_ONLY: st->finalRes = sqrt(s[0]) + SMALL_D; break;
+    case FIN_TRUE_RES: st->trueRes = sqrt(s[0]) + SMALL_D; break;
+    case FIN_PCG_WR: {
+        st->wArAold = st->wArA;
+        st->wArA = s[0];
+        // checkSingularity(mag(wArA)), PCG.cpp:107-117
+        if (!(fabs(st->wArA) > SMALL_D)) {
+            st->singular = 1;
+            st->done = 1;
+            break;
+        }
+        if (st->first) {
+            st->useBeta = 0;
+            st->first = 0;
+        } else {
+            st->useBeta = 1;
+            if (st->flexible && K > 1)
+                st->beta = (-st->alpha * s[K > 1 ? 1 : 0]) / st->wArAold;
+            else
+                st->beta = st->wArA / st->wArAold;
+        }
+        break;
+    }
+    case FIN_PCG_ALPHA:
+        st->wApA = s[0];
+        st->alpha = st->wArA / st->wApA;
+        break;
+    case FIN_PCG_RES:
+        st->finalRes = sqrt(s[0]) + SMALL_D;
+        iteration_end(st);
+        break;
+    case FIN_MG_RES:
+        st->finalRes = sqrt(s[0]) + SMALL_D;
+        iteration_end(st);
+        break;
+    case FIN_BICG_INIT:
+        // initial residual; s[1] = rA0.rA of the first iteration
+        st->initRes = sqrt(s[0]) + SMALL_D;
+        st->finalRes = st->initRes;
+        st->rA0rA = 0.0;
+        bicg_rr(st, s[K > 1 ? 1 : 0]);
+        break;
+    case FIN_BICG_ALPHA: st->alpha = st->rA0rA / s[0]; break;
+    case FIN_BICG_S:
+        st->finalRes = sqrt(s[0]) + SMALL_D;
+        // PBiCGStab.cpp:298-349: converged on ||s|| -> x += alpha y,
+        // nIterations()++, return.  `early` gates the rest of the iteration.
+        if (check_conv(st->finalRes, st->initRes, st->tol, st->relTol, st->nIter + 1,
+                       st->minIter)) {
+            st->converged = 1;
+            st->early = 1;
+            st->nIter++;
+        } else {
+            st->converged = 0;
+        }
+        break;
+    case FIN_BICG_OMEGA:
+        st->tAtA = s[0];
+        st->tAsA = s[K > 1 ? 1 : 0];
+        st->omega = st->tAsA / st->tAtA;
+        break;
+    case FIN_BICG_RES:
+        if (st->early) {  // half-step exit finished: x += alpha y is done
+            st->done = 1;
+            break;
+        }
+        // ||r|| and the loop test; s[1] = rA0.r is the next iteration's
+        // rA0rA (PBiCGStab.cpp:155-196), tested for singularity only when the
+        // loop continues
+        st->finalRes = sqrt(s[0]) + SMALL_D;
+        iteration_end(st);
+        if (!st->done) bicg_rr(st, s[K > 1 ? 1 : 0]);
+        break;
+    default: break;
+    }
+}
+
 }  // namespace unapgpu

@@ -2,6 +2,7 @@
 // drivers.  One solve keeps every vector and scalar on the device; the host
 // only enqueues gated iterations (captured once into a CUDA graph) and polls
 // the `done` flag of the device solver state between batches.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -49,6 +50,8 @@ void Matrix::setValues(const double* diag, const double* upper, const double* lo
 // ---- preconditioners -------------------------------------------------------
 namespace {
 
+Step diag_step(int n, const double* rD, const double* r, double* w, int slot);
+
 class NoPrecond : public Precond {
 public:
     explicit NoPrecond(int n) : n(n) {}
@@ -59,8 +62,29 @@ public:
         // identity preconditioner (unapMatrixPrecond.cpp:4-17)
         diag_apply(ex, n, nullptr, r, w, pool ? pool->site(site, st, fin) : RSpec{}, g);
     }
+    bool appendSteps(std::vector<Step>& out, std::vector<LevelRows>&, const double* r, double* w,
+                     int slot, bool* dotFused) override
+    {
+        out.push_back(diag_step(n, nullptr, r, w, slot));
+        *dotFused = true;
+        return true;
+    }
     int n;
 };
+
+// w = rD r (rD == null: w = r) with the partial of w.r in `slot`
+Step diag_step(int n, const double* rD, const double* r, double* w, int slot)
+{
+    Step s;
+    s.op = ST_DIAG;
+    s.single = mega_single_level(n);
+    s.r1 = n;
+    s.a = r;
+    s.c = w;
+    s.e = rD;
+    s.red = slot;
+    return s;
+}
 
 class DiagPrecond : public Precond {
 public:
@@ -77,6 +101,13 @@ public:
                KState* st, int fin, Gate g) override
     {
         diag_apply(ex, n, rD.p, r, w, pool ? pool->site(site, st, fin) : RSpec{}, g);
+    }
+    bool appendSteps(std::vector<Step>& out, std::vector<LevelRows>&, const double* r, double* w,
+                     int slot, bool* dotFused) override
+    {
+        out.push_back(diag_step(n, rD.p, r, w, slot));
+        *dotFused = true;
+        return true;
     }
     int n;
     DevArray<double> rD;
@@ -104,6 +135,43 @@ public:
     {
         dic_apply(ex, L, dilu, rD.p, r, w, pool, site, st, fin, g);
     }
+    bool appendSteps(std::vector<Step>& out, std::vector<LevelRows>& lv, const double* r,
+                     double* w, int slot, bool* dotFused) override
+    {
+        // level 0 of the table is this matrix
+        Rows<double> A = rows64(L);
+        const bool single = mega_single_level(L.n);
+        for (int k = 0; k < L.nWave; ++k) {
+            Step s;
+            s.op = ST_DIC_FWD;
+            s.single = single;
+            s.r0 = L.waveStart[k];
+            s.r1 = L.waveStart[k + 1];
+            s.a = r;
+            s.c = w;
+            s.e = rD.p;
+            s.d = dilu ? A.val : A.valT;
+            out.push_back(s);
+        }
+        bool firstBwd = true;
+        for (int k = L.nWave - 1; k >= 0; --k) {
+            Step s;
+            s.op = ST_DIC_BWD;
+            s.single = single;
+            s.r0 = L.waveStart[k];
+            s.r1 = L.waveStart[k + 1];
+            s.a = r;
+            s.c = w;
+            s.e = rD.p;
+            s.red = slot;
+            s.f0 = firstBwd ? 0 : 1;
+            firstBwd = false;
+            out.push_back(s);
+        }
+        (void)lv;
+        *dotFused = L.nWave > 0;
+        return true;
+    }
     const Level& L;
     bool dilu;
     DevArray<double> dfac, rD;
@@ -123,8 +191,12 @@ std::unique_ptr<Precond> make_ldu_precond(int type, Matrix& A)
 // ---- Krylov driver -------------------------------------------------------------
 enum { S_INIT = 0, S_WR, S_ALPHA, S_RES, S_TRUE, S_BS, S_BOMEGA, S_NSITES };
 
+static std::atomic<int> g_persistent{1};
+int set_default_executor(int persistent) { return g_persistent.exchange(persistent ? 1 : 0); }
+
 Krylov::Krylov(Matrix& A_, Precond* P_, Method m) : A(A_), P(P_), method(m)
 {
+    useMega = g_persistent.load() != 0;
     n = A.n();
     ex.s = A.stream;
     ex.maxBlocks = device_max_blocks();
@@ -218,6 +290,82 @@ void Krylov::enqueueBicgIteration()
                   g1);
 }
 
+// PCG.cpp:35-183 as one step program: init = r = b - A x and its norm, then
+// per iteration the preconditioner's steps, w.r (+ z.q), direction, q = A p
+// with q.p, and the x/r update with r.r, each reduction followed by the
+// scalar finalize the per-launch kernels run in their last block.
+bool Krylov::buildMega()
+{
+    megaTried = true;
+    if (method != Method::PCG) return false;
+    std::vector<Step> steps;
+    std::vector<LevelRows> lv(1);
+    lv[0].r64 = rows64(*A.L);
+    if (A.L->d_val32.p) lv[0].r32 = rows32(*A.L);
+    const bool single = mega_single_level(n);
+    auto scalar = [&](int fin, int slot) {
+        Step s;
+        s.op = ST_SCALAR;
+        s.f0 = fin;
+        s.red = slot;
+        s.r1 = -1;
+        steps.push_back(s);
+    };
+    Step s0;
+    s0.op = ST_RESID_NORM;
+    s0.single = single;
+    s0.a = x.p;
+    s0.b = b.p;
+    s0.c = r.p;
+    s0.red = 4;
+    steps.push_back(s0);
+    scalar(FIN_INIT_RES, 4);
+    const int nInit = (int)steps.size();
+    bool fused = false;
+    if (!P->appendSteps(steps, lv, r.p, z.p, 0, &fused)) return false;
+    if (!fused || flexible) {
+        Step d;
+        d.op = ST_DOT2;
+        d.single = single;
+        d.r1 = n;
+        d.a = z.p;
+        d.b = r.p;
+        d.c = flexible ? z.p : nullptr;
+        d.d = flexible ? q.p : nullptr;
+        d.red = 0;
+        steps.push_back(d);
+    }
+    scalar(FIN_PCG_WR, 0);
+    Step dir;
+    dir.op = ST_PCG_DIR;
+    dir.r1 = n;
+    dir.a = z.p;
+    dir.c = p.p;
+    steps.push_back(dir);
+    Step mv;
+    mv.op = ST_SPMV_DOT;
+    mv.single = single;
+    mv.a = p.p;
+    mv.c = q.p;
+    mv.red = 2;
+    steps.push_back(mv);
+    scalar(FIN_PCG_ALPHA, 2);
+    Step up;
+    up.op = ST_PCG_UPD;
+    up.r1 = n;
+    up.c = x.p;
+    up.d = r.p;
+    up.a = p.p;
+    up.b = q.p;
+    up.red = 4;
+    steps.push_back(up);
+    scalar(FIN_PCG_RES, 4);
+    mega = std::make_unique<MegaRunner>();
+    mega->setProgram(steps, nInit, lv, 6, ex.s);
+    megaSteps = (int)steps.size();
+    return true;
+}
+
 void Krylov::enqueueIteration()
 {
     if (method == Method::PCG)
@@ -274,7 +422,11 @@ SolveStats Krylov::solveDevice(double* x_ref, const double* b_ref)
     k_to_internal<double>(ex, n, L.d_perm.p, b_ref, b.p);
     initState();
     Rows<double> Ar = rows64(L);
-    if (method == Method::PCG) {
+    if (useMega && !megaTried) megaReady = buildMega();
+    const bool viaMega = useMega && megaReady;
+    if (viaMega) {
+        // the step program's init part computes r = b - A x and its norm
+    } else if (method == Method::PCG) {
         // PCG.cpp:61-75: r = b - A x, initialResidual = normFactor(r)
         k_residual<double>(ex, Ar, x.p, b.p, r.p, pool.site(S_INIT, d_st, FIN_INIT_RES), Gate{});
     } else {
@@ -283,8 +435,15 @@ SolveStats Krylov::solveDevice(double* x_ref, const double* b_ref)
         k_bicg_init(ex, n, b.p, y.p, r.p, r0.p, pool.site(S_INIT, d_st, FIN_BICG_INIT));
     }
     if (n > 0) {
+        bool restarted = false;
         for (;;) {
-            runIterations();
+            if (viaMega) {
+                if (!mega->run(d_st, maxIter + 1, ex.s, restarted))
+                    throw CudaError("step executor: a grid barrier wait timed out");
+                readState();
+            } else {
+                runIterations();
+            }
             if (!trueResidualRestart || h_st->singular || !h_st->converged) break;
             // true residual check: restart from b - A x if the recurrence drifted
             k_residual<double>(ex, Ar, x.p, b.p, z.p, pool.site(S_TRUE, d_st, FIN_TRUE_RES),
@@ -301,6 +460,7 @@ SolveStats Krylov::solveDevice(double* x_ref, const double* b_ref)
             h_st->finalRes = tr;
             h_st->wArA = 1.0e37;
             UNAP_CK(cudaMemcpyAsync(d_st, h_st, sizeof(KState), cudaMemcpyHostToDevice, ex.s));
+            restarted = true;
         }
     }
     k_to_reference<double>(ex, n, L.d_perm.p, x.p, x_ref);

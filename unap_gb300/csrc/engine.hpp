@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "kernels.hpp"
+#include "mega.hpp"
 
 namespace unapgpu {
 
@@ -38,6 +39,16 @@ public:
     virtual bool fusesDot() const { return false; }
     virtual void apply(const Exec& ex, const double* r, double* w, const RedPool* pool, int site,
                        KState* st, int fin, Gate g) = 0;
+    // Step-program form of apply (mega.hpp): appends the steps computing
+    // w = M^-1 r; level 0 of `lv` is the system matrix.  When the steps
+    // also leave w.r in partial slot `slot`, *dotFused is set.  Returns false
+    // when the preconditioner has no step form.
+    virtual bool appendSteps(std::vector<Step>& out, std::vector<LevelRows>& lv, const double* r,
+                             double* w, int slot, bool* dotFused)
+    {
+        (void)out, (void)lv, (void)r, (void)w, (void)slot, (void)dotFused;
+        return false;
+    }
 };
 
 std::unique_ptr<Precond> make_ldu_precond(int type, Matrix& A);  // 1 Diag, 2 DIC, 3 DILU, else none
@@ -54,6 +65,7 @@ public:
     bool flexible = false;   // PCG only
     bool trueResidualRestart = false;  // re-check ||b - Ax|| and restart if needed
     bool useGraph = true;
+    bool useMega = true;     // PCG as one persistent cooperative launch when possible
     // solve on device vectors in reference order (x in/out, b in)
     SolveStats solveDevice(double* x_ref, const double* b_ref);
     // solve on host vectors (copies in and out)
@@ -74,6 +86,10 @@ private:
     cudaGraphExec_t graphExec = nullptr;
     long long graphKernels = 0;
     cudaEvent_t ev0, ev1;
+    std::unique_ptr<MegaRunner> mega;
+    bool megaReady = false, megaTried = false;
+    int megaSteps = 0;
+    bool buildMega();
     void enqueueIteration();
     void enqueuePcgIteration();
     void enqueueBicgIteration();
@@ -81,6 +97,9 @@ private:
     void runIterations();
     void readState();
 };
+
+// default executor of Krylov objects created afterwards; returns the old one
+int set_default_executor(int persistent);
 
 // Dense FP64 SPD inverse by Cholesky (row-major in, row-major out).
 // Returns false when the matrix is not positive definite.
