@@ -230,6 +230,54 @@ int unap_cuda_mg_levels(long int mg, int* nCoarseLevels, int* cells, int maxOut)
 int unap_cuda_mg_solve(long int mg, double* x, const double* b, unap_cuda_stats* stats);
 int unap_cuda_mg_destroy(long int mg);
 
+/* ---- Batched solves of many systems of uneven size.  Systems of at most
+ * 65,536 cells are solved together in one launch (one CTA runs one system's
+ * whole PCG / PBiCGStab solve); larger ones one after another with the
+ * per-system driver.  The CTA size of the fused launch is chosen by the
+ * autotuner (first batch of each size class times 128/256/512/1024
+ * threads).  x and b are device pointers in each system's cell order. */
+typedef struct {
+    long int matrix; /* handle from unap_cuda_matrix_create / ldumatrixcreat_ */
+    int method;      /* 0 PCG, 1 PBiCGStab */
+    int precond;     /* 0 none, 1 Diag, 2 DIC, 3 DILU */
+    double tol, relTol;
+    int maxIter, minIter;
+    double* x;
+    const double* b;
+} unap_cuda_batch_item;
+
+int unap_cuda_batch_create(long int* batch);
+int unap_cuda_batch_solve(long int batch, int count, const unap_cuda_batch_item* items,
+                          unap_cuda_stats* stats, int* ctaThreads);
+int unap_cuda_batch_destroy(long int batch);
+
+/* ---- Continuous-batching solve server.  Requests carry their own matrix
+ * (host arrays, copied) and right-hand side; method 0 mixed AMG-PCG, 1 FP64
+ * AMG-PCG, 2 PCG+DIC, 3 PBiCGStab+DILU.  A request is admitted when a slot
+ * is free and its device-memory estimate fits what the solves in flight
+ * leave of memoryBudget (0: 80% of free memory); maxSlots large solves run
+ * on their own streams so their work overlaps on the GPU; PCG/PBiCGStab
+ * requests of at most smallCells cells are collected and solved together
+ * in one fused launch.  wait() blocks until the request is done, copies x
+ * (host) and reports timings measured from submission. */
+typedef struct {
+    int status;     /* 0 ok */
+    int batched;    /* solved in a fused small-system launch */
+    int nIterations;
+    int converged;
+    double initialResidual, finalResidual;
+    double queueSeconds, setupSeconds, solveSeconds, latencySeconds;
+} unap_cuda_request_info;
+
+int unap_cuda_server_create(long int* server, long long memoryBudget, int maxSlots,
+                            int smallCells);
+int unap_cuda_server_submit(long int server, int nCells, int nFaces, const int* lowerAddr,
+                            const int* upperAddr, const double* lower, const double* diag,
+                            const double* upper, const double* b, int method, double relTol,
+                            int maxIter, long long* id);
+int unap_cuda_server_wait(long int server, long long id, double* x, unap_cuda_request_info* info);
+int unap_cuda_server_destroy(long int server);
+
 int unap_cuda_device_synchronize(void);
 
 /* Kernel timings on the matrix's own stream with CUDA events (the GB300

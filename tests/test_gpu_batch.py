@@ -1,0 +1,71 @@
+"""Batched solves: many systems of uneven size in one fused launch.
+
+Each system's result in the batch must be the same as solved alone (and as
+the oracle's) within the solver tolerance: iteration count within +-1 and
+agreement within 2.2 relTol ||r0|| in residual space.  The batch mixes PCG
+(none/Diag/DIC) on symmetric and PBiCGStab+DILU on nonsymmetric systems, and
+one system above the fused-launch size limit.
+"""
+import numpy as np
+import pytest
+
+from unap_gb300 import capi
+from unap_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def make_batch():
+    rng = np.random.default_rng(41)
+    out = []
+    for i in range(24):
+        e = int(rng.integers(4, 14))
+        kind = i % 4
+        if kind == 0:
+            s = W.laplace(e, e + 1, e + 2, seed=i, permute=True, rhs="normal", shift=0.1)
+            out.append((s, 0, 2))
+        elif kind == 1:
+            s = W.lognormal(e, e, e + 1, seed=i, permute=True, sigma=1.0, shift=0.01)
+            out.append((s, 0, 1))
+        elif kind == 2:
+            s = W.convdiff(e, e, e, seed=i, permute=True, pe=3.0)
+            out.append((s, 1, 3))
+        else:
+            s = W.laplace(e + 2, e, e, seed=i, permute=False, shift=0.5)
+            out.append((s, 0, 0))
+    out.append((W.lognormal(44, 40, 40, seed=99, permute=True, sigma=1.0, shift=0.01), 0, 2))
+    return out
+
+
+def test_batch_matches_individual_and_oracle(cuda, orc):
+    torch = cuda
+    cases = make_batch()
+    mats = [capi.DeviceMatrix(s) for s, _, _ in cases]
+    xs = [torch.zeros(s.n, dtype=torch.float64, device="cuda") for s, _, _ in cases]
+    bs = [torch.tensor(s.b, device="cuda") for s, _, _ in cases]
+    B = capi.Batch()
+    items = [dict(matrix=m, method=meth, precond=pc, x=x, b=b, rel_tol=1e-9, max_iter=2000)
+             for m, (s, meth, pc), x, b in zip(mats, cases, xs, bs)]
+    stats, threads = B.solve(items)
+    assert threads in (128, 256, 512, 1024)
+    for (s, meth, pc), m, x, b, st in zip(cases, mats, xs, bs, stats):
+        x_alone = torch.zeros_like(x)
+        st_alone = m.krylov_solve(meth, pc, x_alone, b, rel_tol=1e-9, max_iter=2000)
+        fn = orc.pcg if meth == 0 else orc.pbicgstab
+        x_ref, st_ref = fn(s, pc, s.b, rel_tol=1e-9, max_iter=2000)
+        assert st["converged"] and st_alone["converged"], (s.name, st)
+        for other in (st_alone["nIterations"], st_ref["n_iter"]):
+            assert abs(st["nIterations"] - other) <= 1, (s.name, st, st_alone, st_ref)
+        xb = x.cpu().numpy()
+        for other in (x_alone.cpu().numpy(), x_ref):
+            d = orc.spmv(s, xb - other)
+            assert np.linalg.norm(d) <= 2.2e-9 * st_ref["init_res"], s.name
+    # a second batch reuses the tuned CTA size and cached factors
+    for x in xs:
+        x.zero_()
+    stats2, threads2 = B.solve(items)
+    assert threads2 == threads
+    assert [s["nIterations"] for s in stats2] == [s["nIterations"] for s in stats]
+    B.close()
+    for m in mats:
+        m.close()

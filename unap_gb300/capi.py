@@ -106,7 +106,113 @@ SIGNATURES = {
     "unap_cuda_mg_levels": (_c_int, [_c_long, _ip, _vp, _c_int]),
     "unap_cuda_mg_solve": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
     "unap_cuda_mg_destroy": (_c_int, [_c_long]),
+    "unap_cuda_batch_create": (_c_int, [_lp]),
+    "unap_cuda_batch_solve": (_c_int, [_c_long, _c_int, _vp, _vp, _ip]),
+    "unap_cuda_batch_destroy": (_c_int, [_c_long]),
+    "unap_cuda_server_create": (_c_int, [_lp, _c_ll, _c_int, _c_int]),
+    "unap_cuda_server_submit": (_c_int, [_c_long, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp,
+                                         _c_int, _c_dbl, _c_int, ctypes.POINTER(_c_ll)]),
+    "unap_cuda_server_wait": (_c_int, [_c_long, _c_ll, _vp, _vp]),
+    "unap_cuda_server_destroy": (_c_int, [_c_long]),
 }
+
+
+class BatchItem(ctypes.Structure):
+    _fields_ = [("matrix", _c_long), ("method", _c_int), ("precond", _c_int), ("tol", _c_dbl),
+                ("relTol", _c_dbl), ("maxIter", _c_int), ("minIter", _c_int), ("x", _vp),
+                ("b", _vp)]
+
+
+class Batch:
+    """Batched solves (``unap_cuda_batch_*``): many systems, one fused launch
+    for the small ones."""
+
+    def __init__(self):
+        h = _c_long(0)
+        check(load().unap_cuda_batch_create(ctypes.byref(h)))
+        self.handle = h.value
+
+    def solve(self, items):
+        """items: list of dicts(matrix=DeviceMatrix, method, precond, x, b,
+        rel_tol=1e-6, tol=0, max_iter=1000, min_iter=0)."""
+        arr = (BatchItem * len(items))()
+        for i, it in enumerate(items):
+            arr[i] = BatchItem(it["matrix"].handle, it.get("method", 0), it.get("precond", 0),
+                               it.get("tol", 0.0), it.get("rel_tol", 1e-6),
+                               it.get("max_iter", 1000), it.get("min_iter", 0),
+                               _ptr(it["x"]), _ptr(it["b"]))
+        stats = (Stats * len(items))()
+        threads = _c_int(0)
+        check(load().unap_cuda_batch_solve(self.handle, len(items), arr, stats,
+                                           ctypes.byref(threads)))
+        return [s.as_dict() for s in stats], threads.value
+
+    def close(self):
+        if self.handle:
+            check(load().unap_cuda_batch_destroy(self.handle))
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("status", _c_int), ("batched", _c_int), ("nIterations", _c_int),
+                ("converged", _c_int), ("initialResidual", _c_dbl), ("finalResidual", _c_dbl),
+                ("queueSeconds", _c_dbl), ("setupSeconds", _c_dbl), ("solveSeconds", _c_dbl),
+                ("latencySeconds", _c_dbl)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+SERVE_METHODS = {"amg_mixed": 0, "amg_fp64": 1, "pcg_dic": 2, "bicgstab_dilu": 3}
+
+
+class Server:
+    """Continuous-batching solve server (``unap_cuda_server_*``)."""
+
+    def __init__(self, memory_budget=0, max_slots=4, small_cells=65536):
+        h = _c_long(0)
+        check(load().unap_cuda_server_create(ctypes.byref(h), memory_budget, max_slots,
+                                             small_cells))
+        self.handle = h.value
+
+    def submit(self, system, method, rel_tol=1e-8, max_iter=1000):
+        l = _i32(system.lower_addr)
+        u = _i32(system.upper_addr)
+        lo = None if system.symm else _f64(system.lower)
+        d = _f64(system.diag)
+        up = _f64(system.upper)
+        b = _f64(system.b)
+        rid = _c_ll(0)
+        m = SERVE_METHODS[method] if isinstance(method, str) else method
+        check(load().unap_cuda_server_submit(self.handle, system.n, system.nf, l.ctypes.data,
+                                             u.ctypes.data,
+                                             None if lo is None else lo.ctypes.data,
+                                             d.ctypes.data, up.ctypes.data, b.ctypes.data, m,
+                                             rel_tol, max_iter, ctypes.byref(rid)))
+        return rid.value
+
+    def wait(self, rid, n):
+        x = np.zeros(n)
+        info = RequestInfo()
+        check(load().unap_cuda_server_wait(self.handle, rid, x.ctypes.data, ctypes.byref(info)))
+        return x, info.as_dict()
+
+    def close(self):
+        if self.handle:
+            check(load().unap_cuda_server_destroy(self.handle))
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class DeviceMG:

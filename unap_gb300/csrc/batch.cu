@@ -1,0 +1,255 @@
+// Batched solves of many LDU systems of uneven size.
+//
+// Systems of at most kBatchSmallCells cells are solved together in ONE
+// launch: one CTA per system runs the whole PCG or PBiCGStab solve
+// (small_solve.cu), so a batch of hundreds of small systems costs one launch
+// instead of hundreds of iterations x kernels.  Larger systems of the batch
+// are solved one after another with the per-system Krylov driver (persistent
+// step executor for PCG).  Vectors enter and leave in the caller's cell
+// order through one batched gather/scatter launch each.
+//
+// The CTA size of the fused launch is picked by an autotuner: the first
+// batch of each size class (largest system rounded up to a power of two) is
+// timed with 128, 256, 512 and 1024 threads per CTA (CUDA events on the
+// batch's stream, x reset between trials) and the fastest is cached for the
+// class.
+#include <algorithm>
+#include <map>
+#include <mutex>
+
+#include "batch.hpp"
+#include "device_common.cuh"
+
+namespace unapgpu {
+
+namespace {
+
+struct PermJob {
+    int n;
+    const int* perm;
+    const double* in;
+    double* out;
+    int toInternal;
+};
+
+// one block per job: out[i] = in[perm[i]] (to internal) or out[perm[i]] = in[i]
+__global__ void batch_perm_kernel(const PermJob* jobs)
+{
+    const PermJob J = jobs[blockIdx.x];
+    for (int i = threadIdx.x; i < J.n; i += blockDim.x) {
+        if (J.toInternal)
+            J.out[i] = J.in[J.perm[i]];
+        else
+            J.out[J.perm[i]] = J.in[i];
+    }
+}
+
+std::mutex g_tune_mutex;
+std::map<int, int> g_tuned;  // size class -> threads
+
+int size_class(int n)
+{
+    int c = 1;
+    while (c < n) c <<= 1;
+    return c;
+}
+
+}  // namespace
+
+int batch_tuned_threads(int sizeClass)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tuned.find(sizeClass);
+    return it == g_tuned.end() ? 0 : it->second;
+}
+
+BatchSolver::BatchSolver(cudaStream_t s) : stream(s) {}
+
+BatchSolver::~BatchSolver() = default;
+
+const double* BatchSolver::factor(Matrix& A, int precond)
+{
+    // reciprocal diagonal for Diag (1/D), DIC or DILU, cached per matrix and
+    // coefficient version
+    Key k{&A, precond};
+    auto it = factors.find(k);
+    if (it != factors.end() && it->second.version == A.L->version) return it->second.rD.p;
+    Fac f;
+    f.version = A.L->version;
+    f.rD.alloc((size_t)A.n());
+    if (precond == 1) {
+        std::vector<double> h((size_t)A.n());
+        for (int i = 0; i < A.n(); ++i) h[(size_t)i] = 1.0 / A.host.diag[(size_t)A.L->perm[(size_t)i]];
+        f.rD.upload(h, stream);
+    } else {
+        DevArray<double> dfac((size_t)A.n());
+        Exec ex{stream, device_max_blocks()};
+        dic_factor(ex, *A.L, precond == 3, dfac.p, f.rD.p);
+        UNAP_CK(cudaStreamSynchronize(stream));
+    }
+    UNAP_CK(cudaStreamSynchronize(stream));
+    auto& slot = factors[k];
+    slot = std::move(f);
+    return slot.rD.p;
+}
+
+std::vector<SolveStats> BatchSolver::solve(const std::vector<BatchItem>& items)
+{
+    std::vector<SolveStats> out(items.size());
+    std::vector<int> small, large;
+    for (size_t i = 0; i < items.size(); ++i) {
+        const BatchItem& it = items[i];
+        if (!it.A->L->sweepable && (it.precond == 2 || it.precond == 3))
+            throw std::invalid_argument("DIC/DILU need oriented, owner-sorted faces");
+        (it.A->n() <= kBatchSmallCells ? small : large).push_back((int)i);
+    }
+    if (!small.empty()) solveSmall(items, small, out);
+    for (int i : large) {
+        const BatchItem& it = items[(size_t)i];
+        auto P = make_ldu_precond(it.precond, *it.A);
+        Krylov K(*it.A, P.get(), it.method == 1 ? Method::PBiCGStab : Method::PCG);
+        K.tol = it.tol;
+        K.relTol = it.relTol;
+        K.maxIter = it.maxIter;
+        K.minIter = it.minIter;
+        out[(size_t)i] = K.solveDevice(it.x, it.b);
+    }
+    return out;
+}
+
+void BatchSolver::solveSmall(const std::vector<BatchItem>& items, const std::vector<int>& idx,
+                             std::vector<SolveStats>& out)
+{
+    const int m = (int)idx.size();
+    size_t total = 0;
+    int nMax = 0;
+    for (int i : idx) {
+        total += (size_t)items[(size_t)i].A->n();
+        nMax = std::max(nMax, items[(size_t)i].A->n());
+    }
+    // workspace: internal x, b and 8 work vectors per system (reused)
+    if (ws.n < total * 10) ws.alloc(total * 10);
+    std::vector<SmallSystem> sys((size_t)m);
+    std::vector<PermJob> in((size_t)2 * m), outJobs((size_t)m);
+    std::vector<std::vector<int>> waves;
+    waveDev.resize((size_t)m);
+    size_t off = 0;
+    for (int j = 0; j < m; ++j) {
+        const BatchItem& it = items[(size_t)idx[(size_t)j]];
+        Matrix& A = *it.A;
+        const int n = A.n();
+        double* xi = ws.p + off;
+        double* bi = xi + n;
+        double* wk = bi + n;
+        off += (size_t)n * 10;
+        SmallSystem& S = sys[(size_t)j];
+        S = SmallSystem{};
+        S.A = rows64(*A.L);
+        S.nWave = A.L->nWave;
+        waveDev[(size_t)j].upload(A.L->waveStart, stream);
+        S.waveStart = waveDev[(size_t)j].p;
+        S.rD = (it.precond >= 1 && it.precond <= 3) ? factor(A, it.precond) : nullptr;
+        S.method = it.method == 1 ? 1 : 0;
+        S.precond = (it.precond >= 1 && it.precond <= 3) ? it.precond : 0;
+        S.tol = it.tol;
+        S.relTol = it.relTol;
+        S.maxIter = it.maxIter;
+        S.minIter = it.minIter;
+        S.zeroX = 0;
+        S.x = xi;
+        S.b = bi;
+        S.work = wk;
+        in[(size_t)2 * j] = PermJob{n, A.L->d_perm.p, it.x, xi, 1};
+        in[(size_t)2 * j + 1] = PermJob{n, A.L->d_perm.p, it.b, bi, 1};
+        outJobs[(size_t)j] = PermJob{n, A.L->d_perm.p, xi, it.x, 0};
+    }
+    if (results.n < (size_t)m) results.alloc((size_t)m);
+    for (int j = 0; j < m; ++j) sys[(size_t)j].result = results.p + j;
+    dSys.upload(sys.data(), sys.size(), stream);
+    dIn.upload(reinterpret_cast<const unsigned char*>(in.data()), in.size() * sizeof(PermJob),
+               stream);
+    dOut.upload(reinterpret_cast<const unsigned char*>(outJobs.data()),
+                outJobs.size() * sizeof(PermJob), stream);
+    if (!capturing()) count_launches(1);
+    batch_perm_kernel<<<2 * m, 256, 0, stream>>>(reinterpret_cast<const PermJob*>(dIn.p));
+
+    const int cls = size_class(nMax);
+    int threads = batch_tuned_threads(cls);
+    if (!threads) threads = autotune(cls, m);
+    launch_small_krylov(stream, dSys.p, m, nullptr, threads);
+    if (!capturing()) count_launches(1);
+    batch_perm_kernel<<<m, 256, 0, stream>>>(reinterpret_cast<const PermJob*>(dOut.p));
+    std::vector<SmallResult> res((size_t)m);
+    UNAP_CK(cudaMemcpyAsync(res.data(), results.p, sizeof(SmallResult) * (size_t)m,
+                            cudaMemcpyDeviceToHost, stream));
+    UNAP_CK(cudaStreamSynchronize(stream));
+    UNAP_CK(cudaGetLastError());
+    for (int j = 0; j < m; ++j) {
+        SolveStats& s = out[(size_t)idx[(size_t)j]];
+        s.nIter = res[(size_t)j].nIter;
+        s.converged = res[(size_t)j].converged;
+        s.singular = res[(size_t)j].singular;
+        s.initRes = res[(size_t)j].initRes;
+        s.finalRes = res[(size_t)j].finalRes;
+    }
+    lastThreads = threads;
+}
+
+int BatchSolver::autotune(int sizeClass, int m)
+{
+    // time each candidate on this batch; x is restored from the gathered
+    // initial guess before every trial (the batch's own solve follows)
+    const int cands[4] = {128, 256, 512, 1024};
+    std::vector<SmallSystem> sys((size_t)m);
+    UNAP_CK(cudaMemcpyAsync(sys.data(), dSys.p, sizeof(SmallSystem) * (size_t)m,
+                            cudaMemcpyDeviceToHost, stream));
+    UNAP_CK(cudaStreamSynchronize(stream));
+    size_t total = 0;
+    for (auto& S : sys) total += (size_t)S.A.n;
+    DevArray<double> x0(total);
+    size_t off = 0;
+    for (auto& S : sys) {
+        UNAP_CK(cudaMemcpyAsync(x0.p + off, S.x, sizeof(double) * (size_t)S.A.n,
+                                cudaMemcpyDeviceToDevice, stream));
+        off += (size_t)S.A.n;
+    }
+    cudaEvent_t e0, e1;
+    UNAP_CK(cudaEventCreate(&e0));
+    UNAP_CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bestT = kSmallBlock;
+    for (int t : cands) {
+        off = 0;
+        for (auto& S : sys) {
+            UNAP_CK(cudaMemcpyAsync(S.x, x0.p + off, sizeof(double) * (size_t)S.A.n,
+                                    cudaMemcpyDeviceToDevice, stream));
+            off += (size_t)S.A.n;
+        }
+        UNAP_CK(cudaEventRecord(e0, stream));
+        launch_small_krylov(stream, dSys.p, m, nullptr, t);
+        UNAP_CK(cudaEventRecord(e1, stream));
+        UNAP_CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        UNAP_CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            bestT = t;
+        }
+    }
+    off = 0;
+    for (auto& S : sys) {
+        UNAP_CK(cudaMemcpyAsync(S.x, x0.p + off, sizeof(double) * (size_t)S.A.n,
+                                cudaMemcpyDeviceToDevice, stream));
+        off += (size_t)S.A.n;
+    }
+    UNAP_CK(cudaStreamSynchronize(stream));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tuned[sizeClass] = bestT;
+    }
+    return bestT;
+}
+
+}  // namespace unapgpu

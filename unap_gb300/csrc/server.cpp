@@ -1,0 +1,256 @@
+// Continuous-batching solve server (see server.hpp).
+#include <chrono>
+
+#include "amg.hpp"
+#include "server.hpp"
+
+namespace unapgpu {
+
+double now_seconds()
+{
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+namespace {
+
+// device-memory estimate of one request (matrix structure, vectors, the AMG
+// hierarchy and its FP32 copies, the dense coarsest inverse)
+size_t estimate_bytes(const ServeRequest& r)
+{
+    const size_t n = (size_t)r.A.n, nf = (size_t)r.A.nf;
+    size_t base = 24 * nf + 112 * n + (r.A.symm ? 0 : 16 * nf);
+    if (r.method == SERVE_AMG_MIXED || r.method == SERVE_AMG_FP64) {
+        base = 2 * base + 8ull * 1000 * 1000;
+        if (r.method == SERVE_AMG_MIXED) base += 2 * 8 * nf + 16 * n;
+    }
+    return base;
+}
+
+}  // namespace
+
+Server::Server(const ServerParams& p) : params(p)
+{
+    if (params.memoryBudget <= 0) {
+        size_t freeB = 0, totalB = 0;
+        UNAP_CK(cudaMemGetInfo(&freeB, &totalB));
+        params.memoryBudget = (long long)(0.8 * (double)freeB);
+    }
+    if (params.maxSlots < 1) params.maxSlots = 1;
+    int dev = 0;
+    UNAP_CK(cudaGetDevice(&dev));
+    for (int i = 0; i < params.maxSlots; ++i)
+        workers.emplace_back([this, dev] {
+            cudaSetDevice(dev);
+            largeWorker();
+        });
+    batchThread = std::thread([this, dev] {
+        cudaSetDevice(dev);
+        batchWorker();
+    });
+}
+
+Server::~Server()
+{
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        stopping = true;
+    }
+    cv.notify_all();
+    for (auto& t : workers) t.join();
+    batchThread.join();
+}
+
+bool Server::admissible(const ServeRequest& r) const
+{
+    // a request larger than the whole budget runs alone
+    if ((long long)r.bytes >= params.memoryBudget) return used.load() == 0;
+    return (long long)(used.load() + r.bytes) <= params.memoryBudget;
+}
+
+long long Server::submit(std::unique_ptr<ServeRequest> r)
+{
+    r->A.validate();
+    if ((int)r->b.size() != r->A.n) throw std::invalid_argument("rhs size differs from nCells");
+    const bool amg = r->method == SERVE_AMG_MIXED || r->method == SERVE_AMG_FP64;
+    if (amg && !r->A.symm) throw std::invalid_argument("AMG-PCG needs a symmetric matrix");
+    r->id = nextId++;
+    r->bytes = estimate_bytes(*r);
+    r->batched = !amg && r->A.n <= params.smallCells;
+    r->tSubmit = now_seconds();
+    const long long id = r->id;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        ServeRequest* raw = r.get();
+        all[id] = std::move(r);
+        (raw->batched ? pendingSmall : pendingLarge).push_back(raw);
+    }
+    cv.notify_all();
+    return id;
+}
+
+std::unique_ptr<ServeRequest> Server::wait(long long id)
+{
+    std::unique_lock<std::mutex> lk(mu);
+    auto it = all.find(id);
+    if (it == all.end()) throw std::invalid_argument("unknown request id");
+    ServeRequest* r = it->second.get();
+    doneCv.wait(lk, [&] { return r->done; });
+    std::unique_ptr<ServeRequest> out = std::move(it->second);
+    all.erase(it);
+    return out;
+}
+
+void Server::finish(ServeRequest* r)
+{
+    r->tEnd = now_seconds();
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        r->done = true;
+    }
+    used -= r->bytes;
+    doneCv.notify_all();
+    cv.notify_all();
+}
+
+void Server::largeWorker()
+{
+    cudaStream_t s = nullptr;
+    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    for (;;) {
+        ServeRequest* r = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv.wait(lk, [&] {
+                return stopping || (!pendingLarge.empty() && admissible(*pendingLarge.front()));
+            });
+            if (pendingLarge.empty() || !admissible(*pendingLarge.front())) {
+                if (stopping) break;
+                continue;
+            }
+            r = pendingLarge.front();
+            pendingLarge.pop_front();
+            used += r->bytes;
+        }
+        r->tStart = now_seconds();
+        try {
+            Matrix A(std::move(r->A), s);
+            const size_t n = (size_t)A.n();
+            DevArray<double> dx(n), db(n);
+            db.upload(r->b, s);
+            dx.zero(s);
+            std::unique_ptr<AmgHierarchy> H;
+            std::unique_ptr<Precond> P;
+            Method m = Method::PCG;
+            bool flexible = false, restart = false;
+            if (r->method == SERVE_AMG_MIXED || r->method == SERVE_AMG_FP64) {
+                AmgParams ap;
+                ap.precision = r->method == SERVE_AMG_MIXED ? 1 : 0;
+                H = std::make_unique<AmgHierarchy>(A, ap);
+                P = std::make_unique<AmgPrecond>(*H);
+                flexible = ap.precision == 1;
+                restart = true;
+            } else if (r->method == SERVE_PCG_DIC) {
+                P = make_ldu_precond(2, A);
+            } else {
+                P = make_ldu_precond(3, A);
+                m = Method::PBiCGStab;
+            }
+            Krylov K(A, P.get(), m);
+            K.relTol = r->relTol;
+            K.maxIter = r->maxIter;
+            K.flexible = flexible;
+            K.trueResidualRestart = restart;
+            // concurrent slots share the SMs: the persistent cooperative
+            // executor needs every SM, so slots use per-step launches
+            K.useMega = params.maxSlots == 1;
+            r->tSetup = now_seconds();
+            r->st = K.solveDevice(dx.p, db.p);
+            r->x.resize(n);
+            UNAP_CK(cudaMemcpyAsync(r->x.data(), dx.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+            UNAP_CK(cudaStreamSynchronize(s));
+        } catch (const std::exception& e) {
+            r->status = -1;
+            r->error = e.what();
+        }
+        finish(r);
+    }
+    if (s) cudaStreamDestroy(s);
+}
+
+void Server::batchWorker()
+{
+    cudaStream_t s = nullptr;
+    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    {
+        BatchSolver B(s);
+        for (;;) {
+            std::vector<ServeRequest*> take;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] {
+                    return stopping || (!pendingSmall.empty() && admissible(*pendingSmall.front()));
+                });
+                while (!pendingSmall.empty() && admissible(*pendingSmall.front())) {
+                    ServeRequest* r = pendingSmall.front();
+                    pendingSmall.pop_front();
+                    used += r->bytes;
+                    take.push_back(r);
+                }
+                if (take.empty()) {
+                    if (stopping) break;
+                    continue;
+                }
+            }
+            const double t0 = now_seconds();
+            std::vector<std::unique_ptr<Matrix>> mats;
+            std::vector<DevArray<double>> xs, bs;
+            std::vector<BatchItem> items;
+            try {
+                for (ServeRequest* r : take) {
+                    r->tStart = t0;
+                    mats.push_back(std::make_unique<Matrix>(std::move(r->A), s));
+                    const size_t n = (size_t)mats.back()->n();
+                    xs.emplace_back(n);
+                    bs.emplace_back(n);
+                    bs.back().upload(r->b, s);
+                    xs.back().zero(s);
+                }
+                for (size_t i = 0; i < take.size(); ++i) {
+                    BatchItem it;
+                    it.A = mats[i].get();
+                    it.method = take[i]->method == SERVE_BICG_DILU ? 1 : 0;
+                    it.precond = take[i]->method == SERVE_BICG_DILU ? 3 : 2;
+                    it.relTol = take[i]->relTol;
+                    it.maxIter = take[i]->maxIter;
+                    it.x = xs[i].p;
+                    it.b = bs[i].p;
+                    items.push_back(it);
+                    take[i]->tSetup = now_seconds();
+                }
+                UNAP_CK(cudaDeviceSynchronize());
+                std::vector<SolveStats> st = B.solve(items);
+                for (size_t i = 0; i < take.size(); ++i) {
+                    ServeRequest* r = take[i];
+                    r->st = st[i];
+                    r->x.resize(xs[i].n);
+                    UNAP_CK(cudaMemcpyAsync(r->x.data(), xs[i].p, xs[i].n * sizeof(double),
+                                            cudaMemcpyDeviceToHost, s));
+                }
+                UNAP_CK(cudaStreamSynchronize(s));
+            } catch (const std::exception& e) {
+                for (ServeRequest* r : take) {
+                    r->status = -1;
+                    r->error = e.what();
+                }
+            }
+            mats.clear();
+            xs.clear();
+            bs.clear();
+            for (ServeRequest* r : take) finish(r);
+        }
+    }
+    if (s) cudaStreamDestroy(s);
+}
+
+}  // namespace unapgpu

@@ -184,8 +184,9 @@ __device__ void small_bicgstab(const SmallSystem& S, SmallResult& R)
     }
 }
 
-__global__ void __launch_bounds__(kSmallBlock) small_krylov_kernel(const SmallSystem* systems,
-                                                                   const KState* gate)
+template <int NT>
+__global__ void __launch_bounds__(NT) small_krylov_kernel(const SmallSystem* systems,
+                                                          const KState* gate)
 {
     if (gate && gate->done) return;
     const SmallSystem S = systems[blockIdx.x];
@@ -204,11 +205,16 @@ __global__ void __launch_bounds__(kSmallBlock) small_krylov_kernel(const SmallSy
 }  // namespace
 
 void launch_small_krylov(cudaStream_t s, const SmallSystem* d_systems, int count,
-                         const KState* gate)
+                         const KState* gate, int threads)
 {
     if (count <= 0) return;
     if (!capturing()) count_launches(1);
-    small_krylov_kernel<<<count, kSmallBlock, 0, s>>>(d_systems, gate);
+    switch (threads) {
+    case 128: small_krylov_kernel<128><<<count, 128, 0, s>>>(d_systems, gate); break;
+    case 256: small_krylov_kernel<256><<<count, 256, 0, s>>>(d_systems, gate); break;
+    case 1024: small_krylov_kernel<1024><<<count, 1024, 0, s>>>(d_systems, gate); break;
+    default: small_krylov_kernel<512><<<count, 512, 0, s>>>(d_systems, gate); break;
+    }
 }
 
 }  // namespace unapgpu

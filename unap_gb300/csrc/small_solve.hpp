@@ -28,8 +28,9 @@ struct SmallSystem {
     SmallResult* result;        // may be null
 };
 
-// One block per system; skipped when gate->done is set.
+// One block of `threads` (128, 256, 512 or 1024) per system; skipped when
+// gate->done is set.
 void launch_small_krylov(cudaStream_t s, const SmallSystem* d_systems, int count,
-                         const KState* gate);
+                         const KState* gate, int threads = kSmallBlock);
 
 }  // namespace unapgpu

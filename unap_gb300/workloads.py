@@ -180,6 +180,55 @@ def _rhs(rng, n, kind):
     raise ValueError(kind)
 
 
+@dataclasses.dataclass
+class Request:
+    arrival: float  # seconds after the stream starts
+    system: LduSystem
+    method: str     # amg_mixed | pcg_dic | bicgstab_dilu
+    seed: int
+
+
+def grid_for(cells: int, rng) -> tuple[int, int, int]:
+    """A cubic or elongated (aspect up to 4:1:1) hex grid of about `cells`."""
+    if rng.random() < 0.5:
+        e = max(4, int(round(cells ** (1 / 3))))
+        return e, e, e
+    aspect = rng.uniform(2.0, 4.0)
+    e = max(4, int(round((cells / aspect) ** (1 / 3))))
+    dims = [max(4, int(round(e * aspect))), e, e]
+    rng.shuffle(dims)
+    return int(dims[0]), int(dims[1]), int(dims[2])
+
+
+def serving_requests(count: int = 2000, rate: float = 200.0, min_cells: int = 8_000,
+                     max_cells: int = 2_000_000, seed: int = 0) -> list[Request]:
+    """The serving stream (config c5): Poisson arrivals at `rate` per second,
+    sizes log-uniform in [min_cells, max_cells], permuted LDU on cubic or
+    elongated grids; 60% log-normal Poisson solved by mixed AMG-PCG, 25%
+    Laplacian by PCG+DIC, 15% convection-diffusion (Pe ~ U[1, 10]) by
+    PBiCGStab+DILU."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(count):
+        t += rng.exponential(1.0 / rate)
+        cells = float(np.exp(rng.uniform(np.log(min_cells), np.log(max_cells))))
+        nx, ny, nz = grid_for(int(cells), rng)
+        u = rng.random()
+        s_seed = int(rng.integers(1 << 31))
+        if u < 0.60:
+            s = lognormal(nx, ny, nz, seed=s_seed, permute=True, sigma=2.0)
+            method = "amg_mixed"
+        elif u < 0.85:
+            s = laplace(nx, ny, nz, seed=s_seed, permute=True, rhs="uniform")
+            method = "pcg_dic"
+        else:
+            s = convdiff(nx, ny, nz, seed=s_seed, permute=True, pe=float(rng.uniform(1, 10)))
+            method = "bicgstab_dilu"
+        out.append(Request(t, s, method, s_seed))
+    return out
+
+
 def config(name: str, scale: float = 1.0, seed: int = 0) -> LduSystem:
     """The benchmark configurations by name, optionally shrunk by `scale`
     (grid edge multiplied by scale, at least 4):
