@@ -227,6 +227,83 @@ def reference_arm(args, rank, dist):
     print(json.dumps(line), flush=True)
 
 
+def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 4):
+    """Config c5 served: a seeded Poisson request stream (200 req/s, sizes
+    log-uniform 8k-2M cells, 60% mixed AMG-PCG / 25% PCG+DIC / 15%
+    PBiCGStab+DILU, tol 1e-8) submitted on its arrival schedule to the
+    continuous-batching server, then the same requests one at a time with
+    the plain FP64 path (FP64 AMG-PCG instead of mixed) on the same GPU.
+    Latency = completion - scheduled arrival."""
+    import torch
+    from unap_gb300 import capi
+    from unap_gb300 import workloads as W
+
+    reqs = W.serving_requests(count=n_requests, rate=200.0, seed=seed)
+    srv = capi.Server(max_slots=max_slots)
+    t0 = time.perf_counter()
+    ids = []
+    for r in reqs:
+        dt = r.arrival - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        ids.append(srv.submit(r.system, r.method, rel_tol=1e-8, max_iter=2000))
+    lat, batched = [], 0
+    for r, rid in zip(reqs, ids):
+        _, info = srv.wait(rid, r.system.n)
+        if not info["converged"]:
+            raise RuntimeError(f"served request did not converge: {info}")
+        lat.append(info["latencySeconds"])
+        batched += info["batched"]
+    span = time.perf_counter() - t0
+    srv.close()
+
+    # the plain path: one request at a time, FP64 everywhere
+    seq_lat = []
+    t1 = time.perf_counter()
+    for r in reqs:
+        ts = time.perf_counter()
+        s = r.system
+        A = capi.DeviceMatrix(s)
+        x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+        b = torch.tensor(s.b, device="cuda")
+        if r.method == "amg_mixed":
+            G = capi.DeviceAmg(A, precision=0, rel_tol=1e-8, max_iter=2000)
+            G.solve(x, b)
+            G.close()
+        else:
+            A.krylov_solve(0 if r.method == "pcg_dic" else 1, 2 if r.method == "pcg_dic" else 3,
+                           x, b, rel_tol=1e-8, max_iter=2000)
+        _ = x.cpu()
+        A.close()
+        seq_lat.append(time.perf_counter() - ts)
+    seq_span = time.perf_counter() - t1
+    pct = lambda v, q: float(np.percentile(np.array(v), q))
+    return {"requests": n_requests, "rate_per_s": 200.0,
+            "solves_per_s": n_requests / span, "p50_s": pct(lat, 50), "p99_s": pct(lat, 99),
+            "batched_requests": batched, "slots": max_slots,
+            "one_at_a_time_fp64": {"solves_per_s": n_requests / seq_span,
+                                   "p50_s": pct(seq_lat, 50), "p99_s": pct(seq_lat, 99),
+                                   "latency": "solve time alone, no queueing"}}
+
+
+def kernels_case(args):
+    """Finest-level kernels of the workload's matrix, each launched on its own
+    and timed with CUDA events (SpMV, DIC/DILU, Gauss-Seidel sweeps FP64 and
+    FP32, residual).  No AMG hierarchy is built, so the device holds only the
+    matrix and a few vectors."""
+    import torch
+    from unap_gb300 import capi
+    from unap_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    s = W.config(args.workload, args.scale, seed=0)
+    A = capi.DeviceMatrix(s)
+    prof = A.profile(reps=args.reps)
+    print(json.dumps({"workload": args.workload, "scale": args.scale, "cells": s.n,
+                      "faces": s.nf, "ms": prof, **A.info()}), flush=True)
+    A.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -237,9 +314,18 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="grid edge scale (testing)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-iters", type=int, default=3)
+    ap.add_argument("--serve", type=int, default=0,
+                    help="also serve this many requests of the c5 stream")
+    ap.add_argument("--kernels", action="store_true",
+                    help="only time the finest-level kernels one launch at a time "
+                         "(the small case for kernel profiles) and exit")
+    ap.add_argument("--reps", type=int, default=5, help="repetitions for --kernels")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
+    if args.kernels:
+        kernels_case(args)
+        return
     world, rank, local, dist = dist_setup(args)
     if args.impl == "reference":
         reference_arm(args, rank, dist)
@@ -260,6 +346,11 @@ def main():
     G64 = capi.DeviceAmg(A, precision=0, rel_tol=1e-10, n_coarsest=1000) \
         if wl["precision"] == 1 else G
     info = G.info()
+    tail_rows, single_rows = capi.set_tail_rows(0, 0)
+    capi.set_tail_rows(tail_rows, single_rows)
+    tail_info = {"cluster_ctas": capi.tail_cluster_size(), "tail_rows": tail_rows,
+                 "single_cta_rows": single_rows,
+                 "levels_in_tail": sum(1 for c in info["cells"][:-1] if c <= tail_rows)}
     b = torch.tensor(s.b, device=device)
     x = torch.zeros(s.n, dtype=torch.float64, device=device)
 
@@ -315,27 +406,33 @@ def main():
         e2e_t.append(time.perf_counter() - t0)
     e2e_v = max_over_ranks(statistics.mean(e2e_t), dist, device)
 
-    # roofline of the dominant kernel: the finest level's FP32 Gauss-Seidel
-    # sweep (all wavefront launches of one sweep), timed with CUDA events on
-    # the matrix's stream right after the timed region
+    # roofline of the dominant kernel: the FP32 (FP64) Gauss-Seidel sweep of
+    # the finest level, all wavefront launches of one sweep timed with CUDA
+    # events on the matrix's stream.  The whole solve's algorithmic bytes
+    # (the library's per-step bookkeeping) over its device time are reported
+    # beside it, with the FP64 SpMV.
     prof = A.profile(reps=10)
     peak, peak_kind = hbm_peak()
-    if wl["precision"] == 1:
-        k_ms = prof["gs_fwd32"]
-        k_bytes = gs32_sweep_bytes(s.n, s.nf)
-        k_name = "gs_kernel<float> (finest-level FP32 Gauss-Seidel sweep)"
-    else:
-        k_ms = prof["gs_fwd"]
-        k_bytes = 32 * s.n + 16 * s.nf
-        k_name = "gs_kernel<double> (finest-level FP64 Gauss-Seidel sweep)"
-    achieved = k_bytes / (k_ms * 1e-3) / 1e9
+    peak_src = ("measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                else "fallback 6.8 TB/s")
+    mixed = wl["precision"] == 1
+    sweep_bytes = gs32_sweep_bytes(s.n, s.nf) if mixed else 32 * s.n + 16 * s.nf
+    sweep_ms = prof["gs_fwd32"] if mixed else prof["gs_fwd"]
+    achieved = sweep_bytes / (sweep_ms * 1e-3) / 1e9
+    spmv = {"kernel": "spmv_kernel<double>", "ms": prof["spmv"],
+            "achieved": spmv64_bytes(s.n, s.nf) / (prof["spmv"] * 1e-3) / 1e9}
+    solve_bytes = stats[-1].get("algorithmicBytes", 0.0)
+    whole = None
+    if solve_bytes > 0:
+        whole = {"algorithmic_bytes": solve_bytes, "s": statistics.mean(dev_s),
+                 "achieved": solve_bytes / statistics.mean(dev_s) / 1e9}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None, "kernel": k_name,
-                "algorithmic_bytes_per_launch": k_bytes, "launch_ms": k_ms,
-                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
-                if peak_kind == "measured" else "fallback 6.8 TB/s",
-                "spmv64": {"achieved": spmv64_bytes(s.n, s.nf) / (prof["spmv"] * 1e-3) / 1e9,
-                           "ms": prof["spmv"]}}
+                "frac": achieved / peak, "traffic": None,
+                "kernel": "gs_kernel<float>" if mixed else "gs_kernel<double>",
+                "launch_group": f"one forward sweep of the finest level "
+                                f"({A.info()['n_wavefronts']} wavefront launches)",
+                "algorithmic_bytes_per_sweep": sweep_bytes, "sweep_ms": sweep_ms,
+                "peak_source": peak_src, "spmv64": spmv, "whole_solve": whole}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -344,6 +441,13 @@ def main():
         except Exception as e:  # reported, never fatal
             cpu = {"value": None, "unit": "s", "cores": 1, "kind": "port",
                    "sample": f"failed: {e}"}
+
+    serving = None
+    if args.serve > 0 and rank == 0:
+        try:
+            serving = serve_bench(args.serve, seed=rank)
+        except Exception as e:  # reported in the line, never fatal
+            serving = {"error": str(e)}
 
     matrix_bytes = A.info()["device_bytes"]
     line = {
@@ -366,8 +470,10 @@ def main():
                    "l2": f"inputs larger than L2: matrix {matrix_bytes / 1e9:.2f} GB on device "
                          f"> {L2_BYTES / 1e6:.0f} MB",
                    "setup_s": info["setup_s"], "wall_s_per_step": t_wall / args.steps,
+                   "vcycle_tail": tail_info,
                    "parallelism": f"replicas x{world}"},
         "fp64": fp64,
+        "serving": serving,
         "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": 2 * 8 * s.n,
                 "d2h_bytes_per_step": 8 * s.n},
         "roofline": roofline,

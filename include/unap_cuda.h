@@ -138,6 +138,8 @@ typedef struct {
     double finalResidual;
     double trueResidual; /* ||b - A x|| + 1e-37 when computed, else -1 */
     double seconds;      /* device time of the solve */
+    double algorithmicBytes; /* DRAM bytes the solve must move (persistent
+                              * executor; 0 otherwise), for roofline use */
 } unap_cuda_stats;
 
 #define UNAP_CUDA_OK 0
@@ -213,6 +215,13 @@ int unap_cuda_amg_info(long int amg, int* nLevels, int* cells, int* wavefronts, 
                        double* setupSeconds, long long* deviceBytes);
 /* one V-cycle z = M^-1 r on device vectors in the caller's cell order */
 int unap_cuda_amg_vcycle(long int amg, const double* r, double* z);
+/* V-cycle timing on the handle's stream: one V-cycle is captured as a CUDA
+ * graph (as inside a solve) with an event node around every level; ms[0] =
+ * mean of `reps` graph launches; ms[1 + k] = level k's own steps in the last
+ * launch (a level that starts the cluster tail holds the whole tail's time,
+ * the levels below it 0).  *written = entries filled.  No counterpart in the
+ * reference. */
+int unap_cuda_amg_profile_vcycle(long int amg, int reps, double* ms, int maxOut, int* written);
 /* AMG-PCG on device vectors (x holds the initial guess) */
 int unap_cuda_amg_solve(long int amg, double* x, const double* b, unap_cuda_stats* stats);
 /* AMG-PCG on host vectors: copies b and x in, solves, copies x out */
@@ -292,12 +301,29 @@ int unap_cuda_profile_kernels(long int handle, int reps, double* ms);
  * launch counts its kernel nodes). */
 long long unap_cuda_launch_count(void);
 
-/* Executor of PCG solves created after the call: 1 (default) runs the whole
+/* Executor of PCG solves created after the call: 0 (default) launches one
+ * kernel per step, one iteration captured as a CUDA graph; 1 runs the whole
  * solve as one persistent cooperative launch that executes a compiled step
- * program; 0 launches one kernel per step, one iteration captured as a CUDA
- * graph.  Both give the same iterates up to dot-product summation order.
- * Returns the previous setting. */
+ * program.  Both give the same iterates up to dot-product summation order.
+ * Returns the previous setting.  No counterpart in the reference. */
 int unap_cuda_set_executor(int persistent);
+
+/* Coarse-level tail of the AMG V-cycle (per-step executor): every level
+ * with at most tailRows rows, down to the dense coarsest solve and back,
+ * runs in one launch of a single thread-block cluster, wavefronts separated
+ * by the cluster barrier; tail levels with at most singleRows rows run on
+ * the cluster's first CTA alone.  tailRows = 0 launches one kernel per
+ * wavefront on every level.  The V-cycle result is bit-identical either
+ * way.  Defaults 2097152 and 2048; the previous values are returned through
+ * the (nullable) pointers.  Applies to V-cycles launched after the call,
+ * CUDA graphs captured before keep their launches.  No counterpart in the
+ * reference. */
+int unap_cuda_set_tail_rows(long long tailRows, long long singleRows, long long* oldTailRows,
+                            long long* oldSingleRows);
+
+/* Cluster size (CTAs) the tail kernel launches with on the current device,
+ * 0 when the device schedules no cluster of 2 or more 1024-thread CTAs. */
+int unap_cuda_tail_cluster_size(int* clusterSize);
 
 /* Failure-detection self-test of the persistent executor's bounded waits:
  * one CTA sleeps (bounded) past a deliberately tiny barrier-wait bound, the

@@ -37,6 +37,27 @@ def executor(request, cuda):
     capi.set_executor(old)
 
 
+TAIL_MODES = {
+    "per-wavefront": (0, 0),            # one kernel per wavefront on every level
+    "cluster": (1 << 40, 0),            # every level in the cluster tail, all CTAs
+    "one-cta": (1 << 40, 1 << 40),      # every level in the tail, first CTA alone
+    "split": (1 << 40, 600),            # cluster levels above 600 rows, one CTA below
+}
+
+
+@pytest.fixture(params=sorted(TAIL_MODES))
+def tail_mode(request, cuda):
+    """Runs a test under each placement of the AMG V-cycle's coarse levels
+    (per-wavefront launches, the cluster tail kernel on all CTAs, on one CTA,
+    and split between the two)."""
+    from unap_gb300 import capi
+    if request.param != "per-wavefront" and capi.tail_cluster_size() < 1:
+        pytest.skip("device schedules no thread-block cluster for the tail kernel")
+    old = capi.set_tail_rows(*TAIL_MODES[request.param])
+    yield request.param
+    capi.set_tail_rows(*old)
+
+
 @pytest.fixture(scope="session")
 def cuda():
     """torch with a CUDA device, and the product library loaded."""

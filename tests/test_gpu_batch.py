@@ -69,3 +69,22 @@ def test_batch_matches_individual_and_oracle(cuda, orc):
     B.close()
     for m in mats:
         m.close()
+
+
+def test_batch_factor_cache_after_matrix_replaced(cuda, orc):
+    """A matrix destroyed and a new one created (the allocator may hand back
+    the same address) must not reuse the old matrix's cached DIC factor."""
+    torch = cuda
+    B = capi.Batch()
+    for seed in range(4):
+        s = W.lognormal(14, 13, 12, seed=100 + seed, permute=True, sigma=1.5, shift=0.01)
+        m = capi.DeviceMatrix(s)
+        x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+        b = torch.tensor(s.b, device="cuda")
+        (st,), _ = B.solve([dict(matrix=m, method=0, precond=2, x=x, b=b, rel_tol=1e-9,
+                                 max_iter=2000)])
+        _, st_ref = orc.pcg(s, 2, s.b, rel_tol=1e-9, max_iter=2000)
+        assert st["converged"], (seed, st)
+        assert abs(st["nIterations"] - st_ref["n_iter"]) <= 1, (seed, st, st_ref)
+        m.close()
+    B.close()

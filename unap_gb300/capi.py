@@ -37,7 +37,7 @@ class UnapCudaError(RuntimeError):
 class Stats(ctypes.Structure):
     _fields_ = [("nIterations", _c_int), ("converged", _c_int), ("singular", _c_int),
                 ("status", _c_int), ("initialResidual", _c_dbl), ("finalResidual", _c_dbl),
-                ("trueResidual", _c_dbl), ("seconds", _c_dbl)]
+                ("trueResidual", _c_dbl), ("seconds", _c_dbl), ("algorithmicBytes", _c_dbl)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -84,11 +84,15 @@ SIGNATURES = {
     "unap_cuda_amg_info": (_c_int, [_c_long, _ip, _vp, _vp, _c_int, _dp,
                                     ctypes.POINTER(_c_ll)]),
     "unap_cuda_amg_vcycle": (_c_int, [_c_long, _vp, _vp]),
+    "unap_cuda_amg_profile_vcycle": (_c_int, [_c_long, _c_int, _vp, _c_int, _ip]),
     "unap_cuda_amg_solve": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
     "unap_cuda_amg_solve_host": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
     "unap_cuda_amg_destroy": (_c_int, [_c_long]),
     "unap_cuda_launch_count": (_c_ll, []),
     "unap_cuda_set_executor": (_c_int, [_c_int]),
+    "unap_cuda_set_tail_rows": (_c_int, [_c_ll, _c_ll, ctypes.POINTER(_c_ll),
+                                         ctypes.POINTER(_c_ll)]),
+    "unap_cuda_tail_cluster_size": (_c_int, [_ip]),
     "unap_cuda_selftest_barrier_timeout": (_c_int, [_ip, _ip]),
     "mgsolversolve_": (None, [_dp, _lp, _dp, _ip, _ip, _ip, _dp, _dp, _ip, _ip, _ip, _dp, _dp]),
     "contruct_solver_mg__": (None, [_lp, _lp, _lp, _dp, _ip, _ip, _ip]),
@@ -258,6 +262,22 @@ def set_executor(persistent: bool) -> bool:
     return bool(load().unap_cuda_set_executor(1 if persistent else 0))
 
 
+def set_tail_rows(tail_rows: int, single_rows: int) -> tuple[int, int]:
+    """Thresholds of the AMG V-cycle's cluster tail kernel (0 disables it);
+    returns the previous (tail_rows, single_rows)."""
+    ot, os_ = _c_ll(), _c_ll()
+    check(load().unap_cuda_set_tail_rows(int(tail_rows), int(single_rows), ctypes.byref(ot),
+                                         ctypes.byref(os_)))
+    return ot.value, os_.value
+
+
+def tail_cluster_size() -> int:
+    """CTAs per cluster of the tail kernel on the current device (0: none)."""
+    c = _c_int()
+    check(load().unap_cuda_tail_cluster_size(ctypes.byref(c)))
+    return c.value
+
+
 class AmgParams(ctypes.Structure):
     _fields_ = [("nCoarsest", _c_int), ("maxLevels", _c_int), ("nPreSweeps", _c_int),
                 ("nPostSweeps", _c_int), ("precision", _c_int), ("flexible", _c_int),
@@ -296,6 +316,14 @@ class DeviceAmg:
 
     def vcycle(self, r, z):
         check(load().unap_cuda_amg_vcycle(self.handle, _ptr(r), _ptr(z)))
+
+    def profile_vcycle(self, reps=10):
+        """Mean V-cycle ms and per-level ms (see unap_cuda_amg_profile_vcycle)."""
+        ms = np.zeros(65)
+        w = _c_int()
+        check(load().unap_cuda_amg_profile_vcycle(self.handle, reps, ms.ctypes.data, 65,
+                                                  ctypes.byref(w)))
+        return {"vcycle_ms": float(ms[0]), "level_ms": ms[1:w.value].tolist()}
 
     def solve(self, x, b):
         st = Stats()

@@ -106,6 +106,17 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
                 cm[(size_t)J * N + I] = inv[(size_t)CL.perm[(size_t)I] * N + CL.perm[(size_t)J]];
         Minv.upload(cm, s);
     }
+    {
+        std::vector<int> all;
+        waveOff.assign((size_t)L + 2, 0);
+        for (int k = 0; k <= L; ++k) {
+            waveOff[(size_t)k] = (int)all.size();
+            const std::vector<int>& w = lv[(size_t)k].L->waveStart;
+            all.insert(all.end(), w.begin(), w.end());
+        }
+        waveOff[(size_t)L + 1] = (int)all.size();
+        dWaves.upload(all, s);
+    }
     for (int k = 0; k <= L; ++k) {
         size_t n = (size_t)lv[(size_t)k].n;
         if (k > 0) {
@@ -121,6 +132,16 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
         }
     }
     UNAP_CK(cudaStreamSynchronize(s));
+    // row-packed copies of the levels the cluster tail may run (in the
+    // precision of the V-cycle)
+    for (int k = 0; k < L; ++k) {
+        if (lv[(size_t)k].n > kTailPackRows) continue;
+        if (params.precision == 1)
+            pack_rows<float>(rows32(*lv[(size_t)k].L), lv[(size_t)k].pack, s);
+        else
+            pack_rows<double>(rows64(*lv[(size_t)k].L), lv[(size_t)k].pack, s);
+    }
+    tail_cluster_size();  // function attributes and the cluster query, outside any capture
     setupSeconds =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -146,7 +167,7 @@ size_t AmgHierarchy::deviceBytes() const
         const Lv& l = lv[k];
         if (l.own) b += l.own->deviceBytes();
         b += l.childStart.bytes() + l.child.bytes() + l.cmap.bytes() + l.x.bytes() + l.b.bytes() +
-             l.r.bytes() + l.xf.bytes() + l.bf.bytes() + l.rf.bytes();
+             l.r.bytes() + l.xf.bytes() + l.bf.bytes() + l.rf.bytes() + l.pack.bytes();
     }
     return b;
 }
@@ -182,14 +203,99 @@ float* AmgHierarchy::R<float>(int k)
     return lv[(size_t)k].rf.p;
 }
 
+int AmgHierarchy::tailFirst(size_t elemBytes) const
+{
+    const int L = nLevels() - 1;
+    const long long rows = tail_rows();
+    if (L < 1 || rows <= 0 || nc > kTailMaxCoarsest) return L;
+    const int C = tail_cluster_size();
+    if (C < 1) return L;
+    const long long single = single_rows();
+    const size_t budget = tail_smem_bytes();
+    // the tail is the suffix of levels with at most `rows` rows whose x fits
+    // in the cluster's shared memory and whose tables fit the kernel's
+    std::vector<int> sizes{nc};
+    int t = L;
+    while (t > 0) {
+        const int k = t - 1;
+        if (lv[(size_t)k].n > rows || !lv[(size_t)k].pack.rec.p || L - k > kTailMaxLevels ||
+            waveOff[(size_t)L] - waveOff[(size_t)k] > kTailMaxWaves)
+            break;
+        std::vector<int> s2{lv[(size_t)k].n};
+        s2.insert(s2.end(), sizes.begin(), sizes.end());
+        const long long e = tail_x_elems(s2, C, single);
+        const size_t bytes = (((size_t)e * elemBytes + 15) & ~(size_t)15) + (size_t)nc * sizeof(double);
+        if (bytes > budget) break;
+        sizes.swap(s2);
+        t = k;
+    }
+    return t;
+}
+
+template <class T>
+void AmgHierarchy::launch_tail(const Exec& ex, int t, Gate g)
+{
+    const int L = nLevels() - 1;
+    const long long single = single_rows();
+    const int C = tail_cluster_size();
+    TailArgs a;
+    a.nLv = L - t;
+    a.nPre = params.nPre;
+    a.nPost = params.nPost;
+    int off = 0;
+    for (int k = t; k < L; ++k) {
+        const Level& Lk = *lv[(size_t)k].L;
+        const Rows<T> rw = rowsT<T>(Lk);
+        const Lv& Cn = lv[(size_t)k + 1];
+        TailLevel& d = a.lv[k - t];
+        d.n = Lk.n;
+        d.nWave = Lk.nWave;
+        d.waveOff = waveOff[(size_t)k] - waveOff[(size_t)t];
+        d.single = Lk.n <= single ? 1 : 0;
+        d.nNext = Cn.n;
+        d.xOff = off;
+        off += (int)tail_x_elems({Lk.n, 0}, C, single);
+        d.sliceOff = rw.sliceOff;
+        d.rowInfo = rw.rowInfo;
+        d.col = rw.col;
+        d.val = rw.val;
+        d.diag = rw.diag;
+        d.b = B<T>(k);
+        d.r = R<T>(k);
+        d.childStart = Cn.childStart.p;
+        d.child = Cn.child.p;
+        d.cmap = Cn.cmap.p;
+        d.pmeta = lv[(size_t)k].pack.meta.p;
+        d.prec = lv[(size_t)k].pack.rec.p;
+    }
+    a.nc = nc;
+    a.xcOff = off;
+    off += (int)tail_x_elems({nc}, C, single);
+    a.xElems = off;
+    a.Minv = Minv.p;
+    a.bc = B<T>(L);
+    a.xOut = X<T>(t);
+    a.waves = dWaves.p + waveOff[(size_t)t];
+    a.nWaveTotal = waveOff[(size_t)L] - waveOff[(size_t)t];
+    a.g = g;
+    launch_tail_vcycle<T>(a, C, ex.s);
+}
+
 template <class T>
 void AmgHierarchy::vcycle_level(const Exec& ex, int k, Gate g)
 {
     const int L = nLevels() - 1;
     T* x = X<T>(k);
     T* b = B<T>(k);
+    if (profIn) UNAP_CK(cudaEventRecordWithFlags((*profIn)[(size_t)k], ex.s, cudaEventRecordExternal));
+    if (k == curTail && k < L) {
+        launch_tail<T>(ex, k, g);
+        if (profOut) UNAP_CK(cudaEventRecordWithFlags((*profOut)[(size_t)k], ex.s, cudaEventRecordExternal));
+        return;
+    }
     if (k == L) {
         k_dense_apply<T>(ex, nc, Minv.p, b, x, g);
+        if (profOut) UNAP_CK(cudaEventRecordWithFlags((*profOut)[(size_t)k], ex.s, cudaEventRecordExternal));
         return;
     }
     const Level& Lk = *lv[(size_t)k].L;
@@ -206,6 +312,7 @@ void AmgHierarchy::vcycle_level(const Exec& ex, int k, Gate g)
     vcycle_level<T>(ex, k + 1, g);
     k_prolong_add<T>(ex, Lk.n, C.cmap.p, X<T>(k + 1), x, g);
     for (int s = 0; s < params.nPost; ++s) gs_sweep<T>(ex, Lk, Rk, x, b, true, false, g);
+    if (profOut) UNAP_CK(cudaEventRecordWithFlags((*profOut)[(size_t)k], ex.s, cudaEventRecordExternal));
 }
 
 template <class T>
@@ -230,6 +337,7 @@ void AmgHierarchy::append_level(std::vector<Step>& out, int k, int tableBase)
         s.e = Minv.p;
         s.a = b;
         s.c = x;
+        s.bytes = 8.0 * nc * nc + 2.0 * sizeof(T) * nc;
         out.push_back(s);
         return;
     }
@@ -244,12 +352,14 @@ void AmgHierarchy::append_level(std::vector<Step>& out, int k, int tableBase)
                 s.f0 = sw == 0 ? 1 : 0;  // first sweep from x = 0: upper side is zero
                 s.b = b;
                 s.c = x;
+                s.bytes = sweep_bytes(s.r1 - s.r0, Lk.n, Lk.nf, prec == 1);
                 out.push_back(s);
             }
     } else {
         Step s = step(ST_FILL0, single);
         s.r1 = Lk.n;
         s.c = x;
+        s.bytes = (double)sizeof(T) * Lk.n;
         out.push_back(s);
     }
     {
@@ -257,6 +367,7 @@ void AmgHierarchy::append_level(std::vector<Step>& out, int k, int tableBase)
         s.a = x;
         s.b = b;
         s.c = R<T>(k);
+        s.bytes = sweep_bytes(Lk.n, Lk.n, Lk.nf, prec == 1);
         out.push_back(s);
     }
     const Lv& C = lv[(size_t)k + 1];
@@ -267,6 +378,7 @@ void AmgHierarchy::append_level(std::vector<Step>& out, int k, int tableBase)
         s.i1 = C.child.p;
         s.a = R<T>(k);
         s.c = B<T>(k + 1);
+        s.bytes = (sizeof(T) + 4.0) * Lk.n + (sizeof(T) + 4.0) * C.n;
         out.push_back(s);
     }
     append_level<T>(out, k + 1, tableBase);
@@ -276,6 +388,7 @@ void AmgHierarchy::append_level(std::vector<Step>& out, int k, int tableBase)
         s.i0 = C.cmap.p;
         s.a = X<T>(k + 1);
         s.c = x;
+        s.bytes = (2.0 * sizeof(T) + 4.0) * Lk.n + (double)sizeof(T) * C.n;
         out.push_back(s);
     }
     for (int sw = 0; sw < params.nPost; ++sw)
@@ -285,6 +398,7 @@ void AmgHierarchy::append_level(std::vector<Step>& out, int k, int tableBase)
             s.r1 = Lk.waveStart[(size_t)w + 1];
             s.b = b;
             s.c = x;
+            s.bytes = sweep_bytes(s.r1 - s.r0, Lk.n, Lk.nf, prec == 1);
             out.push_back(s);
         }
 }
@@ -310,6 +424,7 @@ void AmgHierarchy::appendVcycle(std::vector<Step>& out, std::vector<LevelRows>& 
         s.r1 = n0;
         s.a = r;
         s.c = lv[0].bf.p;
+        s.bytes = 12.0 * n0;
         out.push_back(s);
         append_level<float>(out, 0, tableBase);
         Step t;
@@ -318,6 +433,7 @@ void AmgHierarchy::appendVcycle(std::vector<Step>& out, std::vector<LevelRows>& 
         t.r1 = n0;
         t.a = lv[0].xf.p;
         t.c = z;
+        t.bytes = 12.0 * n0;
         out.push_back(t);
     } else {
         append_level<double>(out, 0, tableBase);
@@ -328,6 +444,7 @@ void AmgHierarchy::vcycle(const Exec& ex, const double* r, double* z, Gate g)
 {
     g_ext.r = r;
     g_ext.z = z;
+    curTail = tailFirst(params.precision == 1 ? sizeof(float) : sizeof(double));
     if (params.precision == 1) {
         k_d2f(ex, lv[0].n, r, lv[0].bf.p);
         vcycle_level<float>(ex, 0, g);
@@ -335,6 +452,82 @@ void AmgHierarchy::vcycle(const Exec& ex, const double* r, double* z, Gate g)
     } else {
         vcycle_level<double>(ex, 0, g);
     }
+}
+
+int AmgHierarchy::profile(cudaStream_t s, int reps, double* ms, int maxOut)
+{
+    const int nl = nLevels();
+    const size_t n0 = (size_t)lv[0].n;
+    DevArray<double> r(n0), z(n0);
+    Exec ex{s, device_max_blocks()};
+    k_fill<double>(ex, (int)n0, r.p, 1.0);
+    cudaEvent_t e0, e1;
+    UNAP_CK(cudaEventCreate(&e0));
+    UNAP_CK(cudaEventCreate(&e1));
+    std::vector<cudaEvent_t> in((size_t)nl), out((size_t)nl);
+    for (int k = 0; k < nl; ++k) {
+        UNAP_CK(cudaEventCreate(&in[(size_t)k]));
+        UNAP_CK(cudaEventCreate(&out[(size_t)k]));
+    }
+    // levels below a tail record no events: start them at the tail's time
+    const int tail = tailFirst(params.precision == 1 ? sizeof(float) : sizeof(double));
+    // one V-cycle captured as a CUDA graph (as inside a solve), with an
+    // event node around every level
+    cudaGraph_t gr = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    profIn = &in;
+    profOut = &out;
+    UNAP_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    set_capturing(true);
+    try {
+        vcycle(ex, r.p, z.p, Gate{});
+    } catch (...) {
+        set_capturing(false);
+        profIn = profOut = nullptr;
+        cudaStreamEndCapture(s, &gr);
+        if (gr) cudaGraphDestroy(gr);
+        throw;
+    }
+    set_capturing(false);
+    profIn = profOut = nullptr;
+    UNAP_CK(cudaStreamEndCapture(s, &gr));
+    UNAP_CK(cudaGraphInstantiate(&ge, gr, 0));
+    UNAP_CK(cudaGraphLaunch(ge, s));
+    UNAP_CK(cudaEventRecord(e0, s));
+    for (int i = 0; i < reps; ++i) UNAP_CK(cudaGraphLaunch(ge, s));
+    UNAP_CK(cudaEventRecord(e1, s));
+    UNAP_CK(cudaEventSynchronize(e1));
+    float t = 0;
+    UNAP_CK(cudaEventElapsedTime(&t, e0, e1));
+    if (maxOut > 0) ms[0] = (double)t / std::max(reps, 1);
+    UNAP_CK(cudaStreamSynchronize(s));
+    cudaGraphExecDestroy(ge);
+    cudaGraphDestroy(gr);
+    int written = 1;
+    for (int k = 0; k < nl && 1 + k < maxOut; ++k) {
+        double own = 0;
+        if (k <= tail || k == nl - 1) {
+            float a = 0, b = 0;
+            const bool inner = k + 1 < nl && !(k == tail && tail < nl - 1);
+            if (inner) {
+                UNAP_CK(cudaEventElapsedTime(&a, in[(size_t)k], in[(size_t)k + 1]));
+                UNAP_CK(cudaEventElapsedTime(&b, out[(size_t)k + 1], out[(size_t)k]));
+                own = (double)a + (double)b;
+            } else if (k <= tail || tail == nl - 1) {
+                UNAP_CK(cudaEventElapsedTime(&a, in[(size_t)k], out[(size_t)k]));
+                own = a;
+            }
+        }
+        ms[1 + k] = own;
+        written = 2 + k;
+    }
+    for (int k = 0; k < nl; ++k) {
+        cudaEventDestroy(in[(size_t)k]);
+        cudaEventDestroy(out[(size_t)k]);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return written;
 }
 
 }  // namespace unapgpu

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "engine.hpp"
+#include "tail.hpp"
 
 namespace unapgpu {
 
@@ -45,6 +46,11 @@ public:
     std::vector<int> levelWavefronts() const;
     // z = M^-1 r, internal order of the finest level
     void vcycle(const Exec& ex, const double* r, double* z, Gate g);
+    // mean V-cycle time over `reps` runs on internal vectors (ms[0]), then
+    // per level from one run with events around every level (ms[1 + k]:
+    // level k's own steps; a level running in the cluster tail holds the
+    // whole tail's time and the levels below it 0); returns levels written
+    int profile(cudaStream_t s, int reps, double* ms, int maxOut);
     // the same V-cycle as a step program (mega.hpp); lv[0] is the finest
     void appendVcycle(std::vector<Step>& out, std::vector<LevelRows>& lv, const double* r,
                       double* z);
@@ -60,15 +66,27 @@ public:
         DevArray<int> cmap;               // prolongation from this level (k >= 1)
         DevArray<double> x, b, r;
         DevArray<float> xf, bf, rf;
+        PackedRows pack;  // row-packed copy for the cluster tail (coarse levels)
     };
     std::vector<Lv> lv;
     DevArray<double> Minv;  // coarsest dense inverse, column-major
     int nc = 0;
+    DevArray<int> dWaves;       // wave starts of every level, concatenated
+    std::vector<int> waveOff;   // level k's first entry in dWaves (size levels + 1)
+    // first level of the V-cycle that runs in the cluster tail kernel under
+    // the current thresholds and shared-memory capacity for elements of
+    // elemBytes bytes (nLevels() - 1: no tail)
+    int tailFirst(size_t elemBytes) const;
 
 private:
     Matrix& A;
     template <class T>
     void vcycle_level(const Exec& ex, int k, Gate g);
+    template <class T>
+    void launch_tail(const Exec& ex, int t, Gate g);
+    int curTail = -1;
+    std::vector<cudaEvent_t>* profIn = nullptr;   // per-level events (profiling)
+    std::vector<cudaEvent_t>* profOut = nullptr;
     template <class T>
     void append_level(std::vector<Step>& out, int k, int tableBase);
     template <class T>

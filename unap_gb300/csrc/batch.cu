@@ -93,6 +93,12 @@ const double* BatchSolver::factor(Matrix& A, int precond)
     return slot.rD.p;
 }
 
+void BatchSolver::forget(const Matrix* A)
+{
+    for (auto it = factors.begin(); it != factors.end();)
+        it = it->first.A == A ? factors.erase(it) : std::next(it);
+}
+
 std::vector<SolveStats> BatchSolver::solve(const std::vector<BatchItem>& items)
 {
     std::vector<SolveStats> out(items.size());

@@ -28,6 +28,9 @@ public:
     std::vector<SolveStats> solve(const std::vector<BatchItem>& items);
     int lastThreads = 0;  // CTA size of the last fused launch
 
+    // drop the cached preconditioner diagonals of a matrix that is going away
+    void forget(const Matrix* A);
+
 private:
     struct Key {
         const Matrix* A;

@@ -109,6 +109,7 @@ void put_stats(const SolveStats& s, unap_cuda_stats* o)
     o->finalResidual = s.finalRes;
     o->trueResidual = s.trueRes;
     o->seconds = s.seconds;
+    o->algorithmicBytes = s.bytes;
 }
 
 // coo2ldu (matrixConversion/coo2ldu.cpp:3-113) after reorderCOO

@@ -61,6 +61,7 @@ void put(const SolveStats& s, unap_cuda_stats* o)
     o->finalResidual = s.finalRes;
     o->trueResidual = s.trueRes;
     o->seconds = s.seconds;
+    o->algorithmicBytes = s.bytes;
 }
 
 }  // namespace
@@ -145,6 +146,16 @@ int unap_cuda_amg_vcycle(long int amg, const double* r, double* z)
     });
 }
 
+int unap_cuda_amg_profile_vcycle(long int amg, int reps, double* ms, int maxOut, int* written)
+{
+    return guarded([&] {
+        AmgHandle* h = amg_from(amg);
+        if (reps < 1 || maxOut < 1) throw std::invalid_argument("reps and maxOut must be >= 1");
+        int w = h->H->profile(h->A->stream, reps, ms, maxOut);
+        if (written) *written = w;
+    });
+}
+
 int unap_cuda_amg_solve(long int amg, double* x, const double* b, unap_cuda_stats* stats)
 {
     return guarded([&] {
@@ -178,6 +189,18 @@ int unap_cuda_amg_destroy(long int amg)
 long long unap_cuda_launch_count(void) { return launch_count(); }
 
 int unap_cuda_set_executor(int persistent) { return set_default_executor(persistent); }
+
+int unap_cuda_set_tail_rows(long long tailRows, long long singleRows, long long* oldTailRows,
+                            long long* oldSingleRows)
+{
+    set_tail_rows(tailRows, singleRows, oldTailRows, oldSingleRows);
+    return UNAP_CUDA_OK;
+}
+
+int unap_cuda_tail_cluster_size(int* clusterSize)
+{
+    return guarded([&] { *clusterSize = tail_cluster_size(); });
+}
 
 int unap_cuda_selftest_barrier_timeout(int* timedOut, int* recovered)
 {

@@ -83,8 +83,8 @@ int unap_cuda_batch_solve(long int batch, int count, const unap_cuda_batch_item*
             b.x = it.x;
             b.b = it.b;
         }
-        // the per-matrix streams finish their setup before the batch stream runs
-        UNAP_CK(cudaDeviceSynchronize());
+        // the matrices' own streams finish their setup before the batch runs
+        for (const BatchItem& b : v) UNAP_CK(cudaStreamSynchronize(b.A->stream));
         std::vector<SolveStats> st = h->S->solve(v);
         for (int i = 0; i < count && stats; ++i) {
             stats[i].nIterations = st[(size_t)i].nIter;
@@ -95,6 +95,7 @@ int unap_cuda_batch_solve(long int batch, int count, const unap_cuda_batch_item*
             stats[i].finalResidual = st[(size_t)i].finalRes;
             stats[i].trueResidual = st[(size_t)i].trueRes;
             stats[i].seconds = st[(size_t)i].seconds;
+            stats[i].algorithmicBytes = st[(size_t)i].bytes;
         }
         if (ctaThreads) *ctaThreads = h->S->lastThreads;
     });

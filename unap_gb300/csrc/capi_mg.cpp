@@ -218,6 +218,7 @@ int unap_cuda_mg_solve(long int mg, double* x, const double* b, unap_cuda_stats*
             stats->finalResidual = st.finalRes;
             stats->trueResidual = -1;
             stats->seconds = st.seconds;
+            stats->algorithmicBytes = st.bytes;
         }
     });
 }

@@ -16,6 +16,16 @@ __device__ __forceinline__ T ldg(const T* p)
     return __ldg(p);
 }
 
+// true when the solver state says the kernel has nothing to do (done, or
+// the BiCGStab half-step exit)
+__device__ __forceinline__ bool gate_closed(const Gate& g)
+{
+    if (!g.st) return false;
+    if ((g.mask & 1) && g.st->done) return true;
+    if ((g.mask & 2) && g.st->early) return true;
+    return false;
+}
+
 __device__ __forceinline__ double warp_sum(double v)
 {
 #pragma unroll
@@ -97,58 +107,88 @@ __device__ __forceinline__ int check_conv(double fin, double init, double tol, d
     return ((fin < tol || (rel > SMALL_D && fin <= rel * init)) && iter >= minIter) ? 1 : 0;
 }
 
+// How a kernel reads the vector it multiplies: through the read-only path
+// (only when nothing writes it during the launch), with plain loads (written
+// earlier in the launch by this CTA), or from L2 (written earlier in the
+// launch by other CTAs, after a grid-wide barrier).
+enum XLoad : int { XL_NC = 0, XL_PLAIN = 1, XL_CG = 2 };
+
+template <int XL, class T>
+__device__ __forceinline__ T ldx(const T* p)
+{
+    if constexpr (XL == XL_NC)
+        return __ldg(p);
+    else if constexpr (XL == XL_CG)
+        return __ldcg(p);
+    else
+        return *p;
+}
+
+// Matrix streams of large levels are read once per sweep: ST loads them with
+// the streaming (evict-first) policy so the gathered vector stays in L2.
+template <bool ST, class T>
+__device__ __forceinline__ T lds(const T* p)
+{
+    if constexpr (ST)
+        return __ldcs(p);
+    else
+        return __ldg(p);
+}
+
 // One row of y = A x in the reference's order (lduMatrixSpMV.cpp:83-92):
 // Apsi = 0; += diag psi; then the row's faces in face order.
-template <class T>
-__device__ __forceinline__ T row_apply(const Rows<T>& A, int r, const T* __restrict__ x)
+//
+// Entries are processed in chunks of CK: all index/value loads of a chunk
+// are issued, then all gathers, then the in-order accumulation, so a row of
+// up to CK entries costs two dependent memory round trips.
+template <class T, int XL = XL_NC, bool ST = false, int CK = 8>
+__device__ __forceinline__ T row_apply(const Rows<T>& A, int r, const T* x)
 {
-    const int info = ldg(A.rowInfo + r);
+    const int info = lds<ST>(A.rowInfo + r);
     const int len = info & 0xffff;
     const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
     T acc = T(0);
-    acc += ldg(A.diag + r) * ldg(x + r);
-    // entries in chunks of 8: all loads of a chunk are issued before the
-    // in-order accumulation, so a row's gathers overlap instead of chaining
-    for (int j0 = 0; j0 < len; j0 += 8) {
-        int c[8];
-        T v[8], xv[8];
+    acc += lds<ST>(A.diag + r) * ldx<XL>(x + r);
+    for (int j0 = 0; j0 < len; j0 += CK) {
+        int c[CK];
+        T v[CK], xv[CK];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
+        for (int k = 0; k < CK; ++k) {
             const int e = base + 32 * (j0 + k);
-            c[k] = j0 + k < len ? ldg(A.col + e) : r;
-            v[k] = j0 + k < len ? ldg(A.val + e) : T(0);
+            c[k] = j0 + k < len ? lds<ST>(A.col + e) : r;
+            v[k] = j0 + k < len ? lds<ST>(A.val + e) : T(0);
         }
 #pragma unroll
-        for (int k = 0; k < 8; ++k) xv[k] = ldg(x + c[k]);
+        for (int k = 0; k < CK; ++k) xv[k] = ldx<XL>(x + c[k]);
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
+        for (int k = 0; k < CK; ++k)
             if (j0 + k < len) acc += v[k] * xv[k];
     }
     return acc;
 }
 
 // Subtract a run of a row's entries from acc in entry order, j in [j0, j1):
-// acc -= val[e] * x[col[e]], with the loads of each 8-entry chunk issued
+// acc -= val[e] * x[col[e]], with the loads of each CK-entry chunk issued
 // before the ordered subtractions.  x may be written concurrently by other
 // wavefronts' rows (plain loads, not the read-only path).
-template <class T>
+template <class T, bool ST = false, int CK = 8>
 __device__ __forceinline__ T row_subtract(const Rows<T>& A, const T* coef, int base, int j0,
                                           int j1, const T* x, T acc)
 {
-    for (int jc = j0; jc < j1; jc += 8) {
-        int c[8];
-        T v[8], xv[8];
+    for (int jc = j0; jc < j1; jc += CK) {
+        int c[CK];
+        T v[CK], xv[CK];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
+        for (int k = 0; k < CK; ++k) {
             const int e = base + 32 * (jc + k);
             const bool on = jc + k < j1;
-            c[k] = on ? ldg(A.col + e) : 0;
-            v[k] = on ? ldg(coef + e) : T(0);
+            c[k] = on ? lds<ST>(A.col + e) : 0;
+            v[k] = on ? lds<ST>(coef + e) : T(0);
         }
 #pragma unroll
-        for (int k = 0; k < 8; ++k) xv[k] = jc + k < j1 ? x[c[k]] : T(0);
+        for (int k = 0; k < CK; ++k) xv[k] = jc + k < j1 ? x[c[k]] : T(0);
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
+        for (int k = 0; k < CK; ++k)
             if (jc + k < j1) acc -= v[k] * xv[k];
     }
     return acc;

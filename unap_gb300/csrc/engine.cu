@@ -83,6 +83,7 @@ Step diag_step(int n, const double* rD, const double* r, double* w, int slot)
     s.c = w;
     s.e = rD;
     s.red = slot;
+    s.bytes = (rD ? 24.0 : 16.0) * n;
     return s;
 }
 
@@ -151,6 +152,8 @@ public:
             s.c = w;
             s.e = rD.p;
             s.d = dilu ? A.val : A.valT;
+            // DIC/DILU apply: 40 N + 32 F over both sweeps, half each
+            s.bytes = 0.5 * ((s.r1 - s.r0) * 40.0 + (double)(s.r1 - s.r0) / L.n * L.nf * 32.0);
             out.push_back(s);
         }
         bool firstBwd = true;
@@ -166,6 +169,7 @@ public:
             s.red = slot;
             s.f0 = firstBwd ? 0 : 1;
             firstBwd = false;
+            s.bytes = 0.5 * ((s.r1 - s.r0) * 40.0 + (double)(s.r1 - s.r0) / L.n * L.nf * 32.0);
             out.push_back(s);
         }
         (void)lv;
@@ -191,7 +195,9 @@ std::unique_ptr<Precond> make_ldu_precond(int type, Matrix& A)
 // ---- Krylov driver -------------------------------------------------------------
 enum { S_INIT = 0, S_WR, S_ALPHA, S_RES, S_TRUE, S_BS, S_BOMEGA, S_NSITES };
 
-static std::atomic<int> g_persistent{1};
+// per-step launches in CUDA graphs measured faster than the persistent
+// executor on the 256^3 AMG-PCG solve, so they are the default
+static std::atomic<int> g_persistent{0};
 int set_default_executor(int persistent) { return g_persistent.exchange(persistent ? 1 : 0); }
 
 Krylov::Krylov(Matrix& A_, Precond* P_, Method m) : A(A_), P(P_), method(m)
@@ -294,12 +300,11 @@ void Krylov::enqueueBicgIteration()
 // per iteration the preconditioner's steps, w.r (+ z.q), direction, q = A p
 // with q.p, and the x/r update with r.r, each reduction followed by the
 // scalar finalize the per-launch kernels run in their last block.
-bool Krylov::buildMega()
+bool Krylov::stepProgram(std::vector<Step>& steps, std::vector<LevelRows>& lv, int& nInitOut)
 {
-    megaTried = true;
     if (method != Method::PCG) return false;
-    std::vector<Step> steps;
-    std::vector<LevelRows> lv(1);
+    steps.clear();
+    lv.assign(1, LevelRows{});
     lv[0].r64 = rows64(*A.L);
     if (A.L->d_val32.p) lv[0].r32 = rows32(*A.L);
     const bool single = mega_single_level(n);
@@ -318,6 +323,7 @@ bool Krylov::buildMega()
     s0.b = b.p;
     s0.c = r.p;
     s0.red = 4;
+    s0.bytes = 32.0 * n + 16.0 * A.L->nf;
     steps.push_back(s0);
     scalar(FIN_INIT_RES, 4);
     const int nInit = (int)steps.size();
@@ -333,6 +339,7 @@ bool Krylov::buildMega()
         d.c = flexible ? z.p : nullptr;
         d.d = flexible ? q.p : nullptr;
         d.red = 0;
+        d.bytes = (flexible ? 24.0 : 16.0) * n;
         steps.push_back(d);
     }
     scalar(FIN_PCG_WR, 0);
@@ -341,6 +348,7 @@ bool Krylov::buildMega()
     dir.r1 = n;
     dir.a = z.p;
     dir.c = p.p;
+    dir.bytes = 24.0 * n;
     steps.push_back(dir);
     Step mv;
     mv.op = ST_SPMV_DOT;
@@ -348,6 +356,7 @@ bool Krylov::buildMega()
     mv.a = p.p;
     mv.c = q.p;
     mv.red = 2;
+    mv.bytes = 24.0 * n + 16.0 * A.L->nf;
     steps.push_back(mv);
     scalar(FIN_PCG_ALPHA, 2);
     Step up;
@@ -358,8 +367,24 @@ bool Krylov::buildMega()
     up.a = p.p;
     up.b = q.p;
     up.red = 4;
+    up.bytes = 48.0 * n;
     steps.push_back(up);
     scalar(FIN_PCG_RES, 4);
+    nInitOut = nInit;
+    megaInitBytes = megaIterBytes = 0;
+    for (int i = 0; i < (int)steps.size(); ++i)
+        (i < nInit ? megaInitBytes : megaIterBytes) += steps[(size_t)i].bytes;
+    bytesKnown = true;
+    return true;
+}
+
+bool Krylov::buildMega()
+{
+    megaTried = true;
+    std::vector<Step> steps;
+    std::vector<LevelRows> lv;
+    int nInit = 0;
+    if (!stepProgram(steps, lv, nInit)) return false;
     mega = std::make_unique<MegaRunner>();
     mega->setProgram(steps, nInit, lv, 6, ex.s);
     megaSteps = (int)steps.size();
@@ -476,6 +501,14 @@ SolveStats Krylov::solveDevice(double* x_ref, const double* b_ref)
     out.converged = h_st->converged;
     out.singular = h_st->singular;
     out.status = h_st->status;
+    // algorithmic bytes of the iteration's steps (the same for both executors)
+    if (!bytesKnown && method == Method::PCG) {
+        std::vector<Step> steps;
+        std::vector<LevelRows> lv;
+        int nInit = 0;
+        stepProgram(steps, lv, nInit);
+    }
+    if (bytesKnown) out.bytes = megaInitBytes + (double)out.nIter * megaIterBytes;
     return out;
 }
 

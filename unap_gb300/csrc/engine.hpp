@@ -14,6 +14,7 @@ struct SolveStats {
     double initRes = 0, finalRes = 0, trueRes = -1;
     int converged = 0, singular = 0, status = 0;
     double seconds = 0;  // device time of the solve (CUDA events)
+    double bytes = 0;    // algorithmic DRAM bytes of the solve (step executor)
 };
 
 // A device-resident LDU matrix (one system).  The host copy keeps the
@@ -89,6 +90,11 @@ private:
     std::unique_ptr<MegaRunner> mega;
     bool megaReady = false, megaTried = false;
     int megaSteps = 0;
+    double megaInitBytes = 0, megaIterBytes = 0;  // algorithmic bytes of the program
+    bool bytesKnown = false;
+    // one PCG iteration (and the init part) as a step program; false for
+    // methods or preconditioners without one
+    bool stepProgram(std::vector<Step>& steps, std::vector<LevelRows>& lv, int& nInit);
     bool buildMega();
     void enqueueIteration();
     void enqueuePcgIteration();

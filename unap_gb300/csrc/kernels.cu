@@ -29,14 +29,6 @@ static inline void tick()
     if (!g_capturing) g_launches++;
 }
 
-__device__ __forceinline__ bool gate_closed(const Gate& g)
-{
-    if (!g.st) return false;
-    if ((g.mask & 1) && g.st->done) return true;
-    if ((g.mask & 2) && g.st->early) return true;
-    return false;
-}
-
 // Finalize of a reduction site (the state logic is shared with the
 // persistent step executor, see apply_fin in device_common.cuh).
 template <int K>
@@ -55,7 +47,7 @@ __device__ __forceinline__ void reduce_and_finalize(double (&v)[K], const RSpec&
 // --------------------------------------------------------------------------
 // SELL-32 row helpers
 // --------------------------------------------------------------------------
-template <class T>
+template <class T, int CK>
 __global__ void __launch_bounds__(kBlock) spmv_kernel(Rows<T> A, const T* __restrict__ x,
                                                       T* __restrict__ y, const T* dotWith,
                                                       RSpec red, Gate g)
@@ -63,7 +55,7 @@ __global__ void __launch_bounds__(kBlock) spmv_kernel(Rows<T> A, const T* __rest
     if (gate_closed(g)) return;
     double v[1] = {0.0};
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < A.n; r += gridDim.x * blockDim.x) {
-        T a = row_apply(A, r, x);
+        T a = row_apply<T, XL_NC, true, CK>(A, r, x);
         y[r] = a;
         if (dotWith) v[0] += (double)a * (double)dotWith[r];
     }
@@ -75,11 +67,14 @@ void k_spmv(const Exec& ex, const Rows<T>& A, const T* x, T* y, const T* dotWith
             Gate g)
 {
     if (A.n <= 0) return;
-    tick(), spmv_kernel<T><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, y, red.blockPart ? dotWith : nullptr,
-                                                      red, g);
+    const T* dw = red.blockPart ? dotWith : nullptr;
+    if (A.wide)
+        tick(), spmv_kernel<T, 16><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
+    else
+        tick(), spmv_kernel<T, 8><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
 }
 
-template <class T>
+template <class T, int CK>
 __global__ void __launch_bounds__(kBlock) residual_kernel(Rows<T> A, const T* __restrict__ x,
                                                           const T* __restrict__ b,
                                                           T* __restrict__ r, RSpec red, Gate g)
@@ -87,8 +82,8 @@ __global__ void __launch_bounds__(kBlock) residual_kernel(Rows<T> A, const T* __
     if (gate_closed(g)) return;
     double v[1] = {0.0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
-        T a = row_apply(A, i, x);
-        T ri = ldg(b + i) - a;
+        T a = row_apply<T, XL_NC, true, CK>(A, i, x);
+        T ri = lds<true>(b + i) - a;
         r[i] = ri;
         v[0] += (double)ri * (double)ri;
     }
@@ -99,7 +94,10 @@ template <class T>
 void k_residual(const Exec& ex, const Rows<T>& A, const T* x, const T* b, T* r, RSpec red, Gate g)
 {
     if (A.n <= 0) return;
-    tick(), residual_kernel<T><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, b, r, red, g);
+    if (A.wide)
+        tick(), residual_kernel<T, 16><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, b, r, red, g);
+    else
+        tick(), residual_kernel<T, 8><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, b, r, red, g);
 }
 
 // --------------------------------------------------------------------------
@@ -108,21 +106,21 @@ void k_residual(const Exec& ex, const Rows<T>& A, const T* x, const T* b, T* r, 
 // first, each side in ascending face order, exactly the reference's
 // bPrime accumulation followed by the owner-face loop.
 // --------------------------------------------------------------------------
-template <class T>
+template <class T, int CK>
 __global__ void __launch_bounds__(kBlock) gs_kernel(Rows<T> A, T* x, const T* __restrict__ b,
                                                     int r0, int r1, int skipUpper, Gate g)
 {
     if (gate_closed(g)) return;
     for (int r = r0 + blockIdx.x * blockDim.x + threadIdx.x; r < r1;
          r += gridDim.x * blockDim.x) {
-        const int info = ldg(A.rowInfo + r);
+        const int info = lds<true>(A.rowInfo + r);
         const int len = info & 0xffff;
         const int nLow = info >> 16;
         const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
-        T acc = ldg(b + r);
-        acc = row_subtract<T>(A, A.val, base, 0, nLow, x, acc);
-        if (!skipUpper) acc = row_subtract<T>(A, A.val, base, nLow, len, x, acc);
-        x[r] = acc / ldg(A.diag + r);
+        T acc = lds<true>(b + r);
+        acc = row_subtract<T, true, CK>(A, A.val, base, 0, nLow, x, acc);
+        if (!skipUpper) acc = row_subtract<T, true, CK>(A, A.val, base, nLow, len, x, acc);
+        x[r] = acc / lds<true>(A.diag + r);
     }
 }
 
@@ -131,7 +129,12 @@ void k_gs_rows(const Exec& ex, const Rows<T>& A, T* x, const T* b, int r0, int r
                Gate g)
 {
     if (r1 <= r0) return;
-    tick(), gs_kernel<T><<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, x, b, r0, r1, skipUpper ? 1 : 0, g);
+    if (A.wide)
+        tick(), gs_kernel<T, 16><<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, x, b, r0, r1,
+                                                                      skipUpper ? 1 : 0, g);
+    else
+        tick(), gs_kernel<T, 8><<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, x, b, r0, r1,
+                                                                     skipUpper ? 1 : 0, g);
 }
 
 template <class T>
@@ -547,6 +550,7 @@ __global__ void dense_apply_kernel(int n, const double* __restrict__ M, const T*
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double t = 0.0;
+#pragma unroll 16
         for (int j = 0; j < n; ++j) t += ldg(M + (size_t)j * n + i) * sb[j];
         x[i] = (T)t;
     }
@@ -652,6 +656,7 @@ Rows<double> rows64(const Level& L)
     A.val = L.d_val.p;
     A.valT = L.symm ? L.d_val.p : L.d_valT.p;
     A.diag = L.d_diag.p;
+    A.wide = 2.0 * L.nf > 8.5 * L.n ? 1 : 0;
     return A;
 }
 
@@ -665,6 +670,7 @@ Rows<float> rows32(const Level& L)
     A.val = L.d_val32.p;
     A.valT = L.d_val32.p;
     A.diag = L.d_diag32.p;
+    A.wide = 2.0 * L.nf > 8.5 * L.n ? 1 : 0;
     return A;
 }
 

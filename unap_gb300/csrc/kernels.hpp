@@ -15,6 +15,7 @@ struct Rows {
     const T* val = nullptr;   // A[row][col]
     const T* valT = nullptr;  // transposed coefficient (== val when symmetric)
     const T* diag = nullptr;
+    int wide = 0;  // rows average more than 8 entries: 16-entry load chunks
 };
 
 Rows<double> rows64(const Level& L);

@@ -1,11 +1,18 @@
 // Host-side construction of one device Level (see unap_internal.hpp).
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <numeric>
 
 #include "unap_internal.hpp"
 
 namespace unapgpu {
+
+// Coefficient versions are unique across all Levels of the process, so a
+// cache keyed by (matrix address, version) cannot match a new matrix that
+// happens to reuse a freed one's address.
+static std::atomic<int> g_version{0};
+static int next_version() { return ++g_version; }
 
 void HostLdu::validate()
 {
@@ -78,6 +85,7 @@ std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key
                                    bool identityOrder, cudaStream_t s)
 {
     auto L = std::make_unique<Level>();
+    L->version = next_version();
     const int n = A.n, nf = A.nf;
     L->n = n;
     L->nf = nf;
@@ -241,7 +249,7 @@ void update_level_values(Level& L, const HostLdu& A, cudaStream_t s)
     L.d_diag.upload(diag, s);
     L.d_val32.release();
     L.d_diag32.release();
-    L.version++;
+    L.version = next_version();
     UNAP_CK(cudaStreamSynchronize(s));
 }
 

@@ -114,7 +114,7 @@ __device__ void exec_resid(const Step& s, const LevelRows& L, int first, int str
     const T* x = (const T*)s.a;
     const T* b = (const T*)s.b;
     T* r = (T*)s.c;
-    for (int i = first; i < A.n; i += stride) r[i] = b[i] - row_apply<T>(A, i, x);
+    for (int i = first; i < A.n; i += stride) r[i] = b[i] - row_apply<T, XL_CG>(A, i, x);
 }
 
 template <class T>
@@ -149,6 +149,7 @@ __device__ void exec_dense(const Step& s, int first, int stride, bool single)
     __syncthreads();
     for (int i = first; i < n; i += stride) {
         double t = 0.0;
+#pragma unroll 16
         for (int j = 0; j < n; ++j) t += ldg(M + (size_t)j * n + i) * sb[j];
         x[i] = (T)t;
     }
@@ -277,7 +278,7 @@ __device__ void exec_step(const Step& s, const MegaArgs& g, bool single)
         double* q = (double*)s.c;
         double v[1] = {0.0};
         for (int i = first; i < A.n; i += stride) {
-            double qi = row_apply<double>(A, i, p);
+            double qi = row_apply<double, XL_CG>(A, i, p);
             q[i] = qi;
             v[0] += qi * p[i];
         }
@@ -291,7 +292,7 @@ __device__ void exec_step(const Step& s, const MegaArgs& g, bool single)
         double* r = (double*)s.c;
         double v[1] = {0.0};
         for (int i = first; i < A.n; i += stride) {
-            double ri = b[i] - row_apply<double>(A, i, x);
+            double ri = b[i] - row_apply<double, XL_CG>(A, i, x);
             r[i] = ri;
             v[0] += ri * ri;
         }

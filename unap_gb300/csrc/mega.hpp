@@ -56,7 +56,19 @@ struct Step {
     const void* e = nullptr;
     const int* i0 = nullptr;
     const int* i1 = nullptr;
+    double bytes = 0;  // algorithmic DRAM bytes of the step (host bookkeeping)
 };
+
+// Algorithmic bytes of a row range of a Gauss-Seidel / residual pass: per
+// cell b, x read, x write, diag; per face one value and two int32 addresses
+// (each LDU array touched once).  FP32 rows: 16 B/cell + 12 B/face; FP64:
+// 32 B/cell + 16 B/face.  A wavefront of `rows` of an n-row level carries
+// rows/n of the level's nf faces.
+inline double sweep_bytes(int rows, int n, int nf, bool fp32)
+{
+    const double cb = fp32 ? 16.0 : 32.0, fb = fp32 ? 12.0 : 16.0;
+    return rows * cb + (n > 0 ? (double)rows / n * nf * fb : 0.0);
+}
 
 struct LevelRows {
     Rows<double> r64;

@@ -162,8 +162,10 @@ void Server::largeWorker()
             K.flexible = flexible;
             K.trueResidualRestart = restart;
             // concurrent slots share the SMs: the persistent cooperative
-            // executor needs every SM, so slots use per-step launches
+            // executor needs every SM, so slots launch their steps directly
+            // (no graph capture, which another slot's setup could invalidate)
             K.useMega = params.maxSlots == 1;
+            K.useGraph = false;
             r->tSetup = now_seconds();
             r->st = K.solveDevice(dx.p, db.p);
             r->x.resize(n);
@@ -228,7 +230,7 @@ void Server::batchWorker()
                     items.push_back(it);
                     take[i]->tSetup = now_seconds();
                 }
-                UNAP_CK(cudaDeviceSynchronize());
+                UNAP_CK(cudaStreamSynchronize(s));
                 std::vector<SolveStats> st = B.solve(items);
                 for (size_t i = 0; i < take.size(); ++i) {
                     ServeRequest* r = take[i];
@@ -244,6 +246,7 @@ void Server::batchWorker()
                     r->error = e.what();
                 }
             }
+            for (auto& m : mats) B.forget(m.get());
             mats.clear();
             xs.clear();
             bs.clear();

@@ -29,7 +29,7 @@ __device__ double blk_dot(int n, const double* a, const double* b)
 
 __device__ void blk_spmv(const Rows<double>& A, const double* x, double* y)
 {
-    for (int i = threadIdx.x; i < A.n; i += blockDim.x) y[i] = row_apply(A, i, x);
+    for (int i = threadIdx.x; i < A.n; i += blockDim.x) y[i] = row_apply<double, XL_PLAIN>(A, i, x);
     __syncthreads();
 }
 

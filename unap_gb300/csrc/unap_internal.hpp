@@ -129,7 +129,7 @@ struct Level {
     // SELL positions of each face's two entries (row u: lower side, row l:
     // upper side), kept to refresh coefficients without rebuilding topology
     std::vector<int> entLo, entUp;
-    int version = 0;  // bumped on every coefficient update
+    int version = 0;  // process-unique, renewed on every coefficient update
     size_t deviceBytes() const;
 };
 
