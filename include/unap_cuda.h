@@ -170,6 +170,18 @@ int unap_cuda_matrix_info(long int handle, int* nWavefronts, long long* nEntries
 
 /* Kernels on device vectors in the caller's cell order (FP64). */
 int unap_cuda_spmv(long int handle, const double* x, double* y);
+/* y = A x like unap_cuda_spmv, for callers that cannot allocate device memory
+ * at call time (a time-stepping code that reserved its whole device-memory
+ * budget up front, or a host thread that must not take the CUDA allocator's
+ * locks).  No counterpart in the reference.  It calls no cudaMalloc/cudaFree:
+ * its scratch is a static device array of 2 x 1,048,576 doubles (16 MiB,
+ * held by every GPU that loads the library until exit), so matrices above
+ * 1,048,576 cells are rejected (UNAP_CUDA_EINVAL).  The handle must already
+ * be built on the device.  The first call on a device looks up the array's
+ * device address; make it before any stream capture begins.  All calls share
+ * the array: calls whose work overlaps on the GPU race; calls on one stream
+ * are safe. */
+int unap_cuda_spmv_noalloc(long int handle, const double* x, double* y);
 /* w = M^-1 r, precond 1 Diag, 2 DIC, 3 DILU */
 int unap_cuda_precondition(long int handle, int precond, const double* r, double* w);
 /* nSweeps Gauss-Seidel sweeps in place on x; backward != 0 sweeps in reverse

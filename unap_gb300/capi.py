@@ -74,6 +74,7 @@ SIGNATURES = {
     "unap_cuda_matrix_info": (_c_int, [_c_long, _ip, ctypes.POINTER(_c_ll),
                                        ctypes.POINTER(_c_ll)]),
     "unap_cuda_spmv": (_c_int, [_c_long, _vp, _vp]),
+    "unap_cuda_spmv_noalloc": (_c_int, [_c_long, _vp, _vp]),
     "unap_cuda_profile_kernels": (_c_int, [_c_long, _c_int, _vp]),
     "unap_cuda_precondition": (_c_int, [_c_long, _c_int, _vp, _vp]),
     "unap_cuda_gauss_seidel": (_c_int, [_c_long, _vp, _vp, _c_int, _c_int]),
