@@ -346,8 +346,7 @@ def main():
     G64 = capi.DeviceAmg(A, precision=0, rel_tol=1e-10, n_coarsest=1000) \
         if wl["precision"] == 1 else G
     info = G.info()
-    tail_rows, single_rows = capi.set_tail_rows(0, 0)
-    capi.set_tail_rows(tail_rows, single_rows)
+    tail_rows, single_rows = capi.get_tail_rows(wl["precision"])
     tail_info = {"cluster_ctas": capi.tail_cluster_size(), "tail_rows": tail_rows,
                  "single_cta_rows": single_rows,
                  "levels_in_tail": sum(1 for c in info["cells"][:-1] if c <= tail_rows)}

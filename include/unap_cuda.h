@@ -320,18 +320,27 @@ long long unap_cuda_launch_count(void);
  * Returns the previous setting.  No counterpart in the reference. */
 int unap_cuda_set_executor(int persistent);
 
-/* Coarse-level tail of the AMG V-cycle (per-step executor): every level
- * with at most tailRows rows, down to the dense coarsest solve and back,
- * runs in one launch of a single thread-block cluster, wavefronts separated
- * by the cluster barrier; tail levels with at most singleRows rows run on
- * the cluster's first CTA alone.  tailRows = 0 launches one kernel per
- * wavefront on every level.  The V-cycle result is bit-identical either
- * way.  Defaults 2097152 and 2048; the previous values are returned through
- * the (nullable) pointers.  Applies to V-cycles launched after the call,
- * CUDA graphs captured before keep their launches.  No counterpart in the
+/* Per-wavefront Gauss-Seidel launches use programmatic dependent launch:
+ * the next wavefront's kernel starts launching while the previous one runs
+ * and loads its rows' matrix data before it waits for it (1, default); 0
+ * launches them one after the other.  Results are identical.  Returns the
+ * previous setting.  No counterpart in the reference. */
+int unap_cuda_set_wave_pdl(int on);
+
+/* Coarse-level tail of the AMG V-cycle (per-step executor), set for the FP64
+ * (precision 0) or FP32 (precision 1) V-cycle: every level with at most
+ * tailRows rows whose iterate fits in the cluster's shared memory, down to
+ * the dense coarsest solve and back, runs in one launch of a single
+ * thread-block cluster, wavefronts separated by the cluster barrier; tail
+ * levels with at most singleRows rows run on the cluster's first CTA alone.
+ * tailRows = 0 launches one kernel per wavefront on every level.  The
+ * V-cycle result is bit-identical either way.  Defaults: FP64 2097152 and
+ * 8192, FP32 32768 and 2^30; the previous values are returned through the
+ * (nullable) pointers.  Applies to V-cycles launched after the call, CUDA
+ * graphs captured before keep their launches.  No counterpart in the
  * reference. */
-int unap_cuda_set_tail_rows(long long tailRows, long long singleRows, long long* oldTailRows,
-                            long long* oldSingleRows);
+int unap_cuda_set_tail_rows(int precision, long long tailRows, long long singleRows,
+                            long long* oldTailRows, long long* oldSingleRows);
 
 /* Cluster size (CTAs) the tail kernel launches with on the current device,
  * 0 when the device schedules no cluster of 2 or more 1024-thread CTAs. */

@@ -55,7 +55,7 @@ def tail_mode(request, cuda):
         pytest.skip("device schedules no thread-block cluster for the tail kernel")
     old = capi.set_tail_rows(*TAIL_MODES[request.param])
     yield request.param
-    capi.set_tail_rows(*old)
+    capi.restore_tail_rows(old)
 
 
 @pytest.fixture(scope="session")

@@ -118,7 +118,7 @@ def test_amg_pcg_same_bits_in_every_tail_mode(cuda, precision):
             results[m] = (st["nIterations"], x.cpu().numpy())
             G.close()
     finally:
-        capi.set_tail_rows(*old)
+        capi.restore_tail_rows(old)
         A.close()
     it0, x0 = results["per-wavefront"]
     for m, (it, xm) in results.items():

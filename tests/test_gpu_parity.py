@@ -77,17 +77,23 @@ def test_preconditioners_bit_exact(cuda, orc):
         A.close()
 
 
-def test_gauss_seidel_bit_exact(cuda, orc):
+@pytest.mark.parametrize("pdl", [True, False])
+def test_gauss_seidel_bit_exact(cuda, orc, pdl):
+    """Wavefront launches with and without programmatic dependent launch."""
     torch = cuda
-    for s in systems():
-        A = capi.DeviceMatrix(s)
-        x0 = np.random.default_rng(s.n + 2).standard_normal(s.n)
-        for backward in (False, True):
-            x = dev(torch, x0)
-            A.gauss_seidel(x, dev(torch, s.b), 3, backward=backward)
-            assert np.array_equal(host(x), orc.gs(s, x0, s.b, 3, backward=backward)), (
-                s.name, backward)
-        A.close()
+    old = capi.set_wave_pdl(pdl)
+    try:
+        for s in systems():
+            A = capi.DeviceMatrix(s)
+            x0 = np.random.default_rng(s.n + 2).standard_normal(s.n)
+            for backward in (False, True):
+                x = dev(torch, x0)
+                A.gauss_seidel(x, dev(torch, s.b), 3, backward=backward)
+                assert np.array_equal(host(x), orc.gs(s, x0, s.b, 3, backward=backward)), (
+                    s.name, backward)
+            A.close()
+    finally:
+        capi.set_wave_pdl(old)
 
 
 def _solution_close(x, x_ref):

@@ -91,7 +91,8 @@ SIGNATURES = {
     "unap_cuda_amg_destroy": (_c_int, [_c_long]),
     "unap_cuda_launch_count": (_c_ll, []),
     "unap_cuda_set_executor": (_c_int, [_c_int]),
-    "unap_cuda_set_tail_rows": (_c_int, [_c_ll, _c_ll, ctypes.POINTER(_c_ll),
+    "unap_cuda_set_wave_pdl": (_c_int, [_c_int]),
+    "unap_cuda_set_tail_rows": (_c_int, [_c_int, _c_ll, _c_ll, ctypes.POINTER(_c_ll),
                                          ctypes.POINTER(_c_ll)]),
     "unap_cuda_tail_cluster_size": (_c_int, [_ip]),
     "unap_cuda_selftest_barrier_timeout": (_c_int, [_ip, _ip]),
@@ -263,13 +264,36 @@ def set_executor(persistent: bool) -> bool:
     return bool(load().unap_cuda_set_executor(1 if persistent else 0))
 
 
-def set_tail_rows(tail_rows: int, single_rows: int) -> tuple[int, int]:
-    """Thresholds of the AMG V-cycle's cluster tail kernel (0 disables it);
-    returns the previous (tail_rows, single_rows)."""
-    ot, os_ = _c_ll(), _c_ll()
-    check(load().unap_cuda_set_tail_rows(int(tail_rows), int(single_rows), ctypes.byref(ot),
-                                         ctypes.byref(os_)))
-    return ot.value, os_.value
+def set_wave_pdl(on: bool) -> bool:
+    """Programmatic dependent launch of wavefront kernels; returns the previous value."""
+    return bool(load().unap_cuda_set_wave_pdl(1 if on else 0))
+
+
+def set_tail_rows(tail_rows: int, single_rows: int, precision: int | None = None):
+    """Thresholds of the AMG V-cycle's cluster tail kernel (0 disables it) for
+    the FP64 (0) or FP32 (1) V-cycle, or both (None).  Returns the previous
+    settings as {precision: (tail_rows, single_rows)}, which
+    restore_tail_rows() puts back."""
+    old = {}
+    for p in ((0, 1) if precision is None else (precision,)):
+        ot, os_ = _c_ll(), _c_ll()
+        check(load().unap_cuda_set_tail_rows(p, int(tail_rows), int(single_rows),
+                                             ctypes.byref(ot), ctypes.byref(os_)))
+        old[p] = (ot.value, os_.value)
+    return old
+
+
+def restore_tail_rows(old) -> None:
+    """Put back settings returned by set_tail_rows()."""
+    for p, (t, s) in old.items():
+        check(load().unap_cuda_set_tail_rows(p, int(t), int(s), None, None))
+
+
+def get_tail_rows(precision: int) -> tuple[int, int]:
+    """Current (tail_rows, single_rows) of the FP64 (0) or FP32 (1) V-cycle."""
+    old = set_tail_rows(0, 0, precision)
+    restore_tail_rows(old)
+    return old[precision]
 
 
 def tail_cluster_size() -> int:

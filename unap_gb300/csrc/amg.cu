@@ -206,11 +206,11 @@ float* AmgHierarchy::R<float>(int k)
 int AmgHierarchy::tailFirst(size_t elemBytes) const
 {
     const int L = nLevels() - 1;
-    const long long rows = tail_rows();
+    const long long rows = tail_rows(params.precision);
     if (L < 1 || rows <= 0 || nc > kTailMaxCoarsest) return L;
     const int C = tail_cluster_size();
     if (C < 1) return L;
-    const long long single = single_rows();
+    const long long single = single_rows(params.precision);
     const size_t budget = tail_smem_bytes();
     // the tail is the suffix of levels with at most `rows` rows whose x fits
     // in the cluster's shared memory and whose tables fit the kernel's
@@ -236,7 +236,7 @@ template <class T>
 void AmgHierarchy::launch_tail(const Exec& ex, int t, Gate g)
 {
     const int L = nLevels() - 1;
-    const long long single = single_rows();
+    const long long single = single_rows(params.precision);
     const int C = tail_cluster_size();
     TailArgs a;
     a.nLv = L - t;

@@ -190,11 +190,12 @@ long long unap_cuda_launch_count(void) { return launch_count(); }
 
 int unap_cuda_set_executor(int persistent) { return set_default_executor(persistent); }
 
-int unap_cuda_set_tail_rows(long long tailRows, long long singleRows, long long* oldTailRows,
-                            long long* oldSingleRows)
+int unap_cuda_set_wave_pdl(int on) { return set_wave_pdl(on); }
+
+int unap_cuda_set_tail_rows(int precision, long long tailRows, long long singleRows,
+                            long long* oldTailRows, long long* oldSingleRows)
 {
-    set_tail_rows(tailRows, singleRows, oldTailRows, oldSingleRows);
-    return UNAP_CUDA_OK;
+    return guarded([&] { set_tail_rows(precision, tailRows, singleRows, oldTailRows, oldSingleRows); });
 }
 
 int unap_cuda_tail_cluster_size(int* clusterSize)

@@ -110,18 +110,74 @@ template <class T, int CK>
 __global__ void __launch_bounds__(kBlock) gs_kernel(Rows<T> A, T* x, const T* __restrict__ b,
                                                     int r0, int r1, int skipUpper, Gate g)
 {
-    if (gate_closed(g)) return;
-    for (int r = r0 + blockIdx.x * blockDim.x + threadIdx.x; r < r1;
-         r += gridDim.x * blockDim.x) {
-        const int info = lds<true>(A.rowInfo + r);
+    // Programmatic dependent launch: the next wavefront's kernel may begin
+    // launching now.  Before griddepcontrol.wait a kernel reads only data no
+    // kernel of the sweep writes (matrix streams and b); x and the solver
+    // state are read after it, when the previous kernel has completed.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    int r = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+    int info = 0, base = 0;
+    T d = T(1), bb = T(0);
+    int c[CK];
+    T v[CK];
+    if (r < r1) {
+        info = lds<true>(A.rowInfo + r);
+        base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
+        d = lds<true>(A.diag + r);
+        bb = lds<true>(b + r);
         const int len = info & 0xffff;
-        const int nLow = info >> 16;
-        const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
+#pragma unroll
+        for (int k = 0; k < CK; ++k) {
+            const int e = base + 32 * k;
+            c[k] = k < len ? lds<true>(A.col + e) : 0;
+            v[k] = k < len ? lds<true>(A.val + e) : T(0);
+        }
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (gate_closed(g)) return;
+    if (r < r1) {
+        const int jEnd = skipUpper ? (info >> 16) : (info & 0xffff);
+        T xv[CK];
+#pragma unroll
+        for (int k = 0; k < CK; ++k) xv[k] = k < jEnd ? x[c[k]] : T(0);
+        T acc = bb;
+#pragma unroll
+        for (int k = 0; k < CK; ++k)
+            if (k < jEnd) acc -= v[k] * xv[k];
+        if (jEnd > CK) acc = row_subtract<T, true, CK>(A, A.val, base, CK, jEnd, x, acc);
+        x[r] = acc / d;
+    }
+    for (r += gridDim.x * blockDim.x; r < r1; r += gridDim.x * blockDim.x) {
+        const int info2 = lds<true>(A.rowInfo + r);
+        const int len = info2 & 0xffff;
+        const int nLow = info2 >> 16;
+        const int base2 = ldg(A.sliceOff + (r >> 5)) + (r & 31);
         T acc = lds<true>(b + r);
-        acc = row_subtract<T, true, CK>(A, A.val, base, 0, nLow, x, acc);
-        if (!skipUpper) acc = row_subtract<T, true, CK>(A, A.val, base, nLow, len, x, acc);
+        acc = row_subtract<T, true, CK>(A, A.val, base2, 0, nLow, x, acc);
+        if (!skipUpper) acc = row_subtract<T, true, CK>(A, A.val, base2, nLow, len, x, acc);
         x[r] = acc / lds<true>(A.diag + r);
     }
+}
+
+static std::atomic<int> g_pdl{1};
+int set_wave_pdl(int on) { return g_pdl.exchange(on ? 1 : 0); }
+
+// one wavefront launch, with programmatic dependent launch when enabled
+template <class T, int CK>
+static void launch_gs(const Exec& ex, const Rows<T>& A, T* x, const T* b, int r0, int r1,
+                      int skipUpper, Gate g)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)ex.grid(r1 - r0));
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = ex.s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = g_pdl.load() ? 1 : 0;
+    tick();
+    UNAP_CK(cudaLaunchKernelEx(&cfg, gs_kernel<T, CK>, A, x, b, r0, r1, skipUpper, g));
 }
 
 template <class T>
@@ -130,11 +186,9 @@ void k_gs_rows(const Exec& ex, const Rows<T>& A, T* x, const T* b, int r0, int r
 {
     if (r1 <= r0) return;
     if (A.wide)
-        tick(), gs_kernel<T, 16><<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, x, b, r0, r1,
-                                                                      skipUpper ? 1 : 0, g);
+        launch_gs<T, 16>(ex, A, x, b, r0, r1, skipUpper ? 1 : 0, g);
     else
-        tick(), gs_kernel<T, 8><<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, x, b, r0, r1,
-                                                                     skipUpper ? 1 : 0, g);
+        launch_gs<T, 8>(ex, A, x, b, r0, r1, skipUpper ? 1 : 0, g);
 }
 
 template <class T>

@@ -107,4 +107,9 @@ void k_scaling_sums(const Exec& ex, int n, const T* source, const T* Acf, T* fie
 template <class T>
 void k_axpby(const Exec& ex, int n, T a, const T* x, T b, T* y, Gate g);  // y = a x + b y
 
+// Wavefront Gauss-Seidel launches use programmatic dependent launch (the
+// next wavefront's kernel launches while the previous one runs and loads its
+// matrix data before waiting); 0 turns it off.  Returns the previous value.
+int set_wave_pdl(int on);
+
 }  // namespace unapgpu

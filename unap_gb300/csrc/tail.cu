@@ -19,8 +19,12 @@ namespace unapgpu {
 
 namespace {
 
-std::atomic<long long> g_tailRows{1ll << 21};
-std::atomic<long long> g_singleRows{2048};
+// per V-cycle precision (0 FP64, 1 FP32), measured on the 256^3 log-normal
+// hierarchy: per-wavefront launches with programmatic dependent launch beat
+// the cluster tail on FP32 levels above ~30k rows; FP64 levels are slower
+// per launch, so the tail pays off from larger levels on
+std::atomic<long long> g_tailRows[2] = {{1ll << 21}, {1ll << 15}};
+std::atomic<long long> g_singleRows[2] = {{8192}, {1ll << 30}};
 
 constexpr int kStaticSmem =
     kTailMaxWaves * 4 + kTailMaxCluster * 4 + kTailMaxLevels * (int)sizeof(TailLevel) + 64;
@@ -563,17 +567,18 @@ long long tail_x_elems(const std::vector<int>& sizes, int C, long long singleRow
     return e;
 }
 
-void set_tail_rows(long long tailRows, long long singleRows, long long* oldTail,
+void set_tail_rows(int precision, long long tailRows, long long singleRows, long long* oldTail,
                    long long* oldSingle)
 {
-    const long long t = g_tailRows.exchange(tailRows < 0 ? 0 : tailRows);
-    const long long s = g_singleRows.exchange(singleRows < 0 ? 0 : singleRows);
+    if (precision != 0 && precision != 1) throw std::invalid_argument("precision must be 0 or 1");
+    const long long t = g_tailRows[precision].exchange(tailRows < 0 ? 0 : tailRows);
+    const long long s = g_singleRows[precision].exchange(singleRows < 0 ? 0 : singleRows);
     if (oldTail) *oldTail = t;
     if (oldSingle) *oldSingle = s;
 }
 
-long long tail_rows() { return g_tailRows.load(); }
-long long single_rows() { return g_singleRows.load(); }
+long long tail_rows(int precision) { return g_tailRows[precision ? 1 : 0].load(); }
+long long single_rows(int precision) { return g_singleRows[precision ? 1 : 0].load(); }
 
 template <class T>
 void launch_tail_vcycle(const TailArgs& a, int C, cudaStream_t s)

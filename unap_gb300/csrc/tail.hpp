@@ -91,14 +91,15 @@ size_t tail_smem_bytes();
 // (the coarsest last); singleRows as in set_tail_rows.
 long long tail_x_elems(const std::vector<int>& sizes, int clusterSize, long long singleRows);
 
-// Tail thresholds (process-wide): levels with at most `tailRows` rows run in
-// the tail kernel (0 disables it) as far as their x fits in shared memory;
-// tail levels with at most `singleRows` rows run on one CTA.  Returns the
-// previous values through the pointers.
-void set_tail_rows(long long tailRows, long long singleRows, long long* oldTail,
+// Tail thresholds (process-wide, per V-cycle precision: 0 FP64, 1 FP32):
+// levels with at most `tailRows` rows run in the tail kernel (0 disables it)
+// as far as their x fits in shared memory; tail levels with at most
+// `singleRows` rows run on one CTA.  Returns the previous values through the
+// pointers.
+void set_tail_rows(int precision, long long tailRows, long long singleRows, long long* oldTail,
                    long long* oldSingle);
-long long tail_rows();
-long long single_rows();
+long long tail_rows(int precision);
+long long single_rows(int precision);
 
 template <class T>
 void launch_tail_vcycle(const TailArgs& a, int clusterSize, cudaStream_t s);
