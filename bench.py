@@ -44,6 +44,9 @@ WORKLOADS = {
                method="amg", precision=0),
 }
 L2_BYTES = 129 * 2 ** 20
+# DRAM bytes / algorithmic bytes of a whole FP32 Gauss-Seidel sweep, measured
+# in situ (no cache flush) with ncu on the 192^3 log-normal matrix
+SWEEP_TRAFFIC_RATIO = 1.32
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -382,12 +385,16 @@ def main():
     # FP64 AMG-PCG on the same matrix (the metric's "mixed vs FP64")
     fp64 = None
     if G64 is not G:
+        x_mixed = x.clone()
         for _ in range(args.warmup):
             solve(G64)
         st64 = [solve(G64) for _ in range(args.steps)]
         t64 = max_over_ranks(statistics.mean(st["seconds"] for st in st64), dist, device)
+        # the mixed solution against the FP64 one (both to a 1e-10 residual)
+        rel = float(torch.linalg.vector_norm(x_mixed - x) / torch.linalg.vector_norm(x))
         fp64 = {"value": t64, "unit": "s", "iterations": st64[-1]["nIterations"],
-                "speedup_mixed_vs_fp64": t64 / per_solve}
+                "speedup_mixed_vs_fp64": t64 / per_solve,
+                "mixed_solution_rel_diff_vs_fp64": rel}
     gpu_iters64 = fp64["iterations"] if fp64 else iters
 
     # e2e: the host-array C ABI call, b/x copies inside the timed region
@@ -426,7 +433,12 @@ def main():
         whole = {"algorithmic_bytes": solve_bytes, "s": statistics.mean(dev_s),
                  "achieved": solve_bytes / statistics.mean(dev_s) / 1e9}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None,
+                "frac": achieved / peak,
+                "traffic": SWEEP_TRAFFIC_RATIO * sweep_bytes if mixed else None,
+                "traffic_source": "in-situ DRAM bytes of a whole FP32 sweep measured by ncu "
+                                  "on the 192^3 case (profiles/gs_kernel_float_c4_192cube_"
+                                  "waves.md), ratio 1.32 to algorithmic, scaled to this sweep"
+                                  if mixed else None,
                 "kernel": "gs_kernel<float>" if mixed else "gs_kernel<double>",
                 "launch_group": f"one forward sweep of the finest level "
                                 f"({A.info()['n_wavefronts']} wavefront launches)",
