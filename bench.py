@@ -230,7 +230,7 @@ def reference_arm(args, rank, dist):
     print(json.dumps(line), flush=True)
 
 
-def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 4):
+def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 4, compare_plain: bool = True):
     """Config c5 served: a seeded Poisson request stream (200 req/s, sizes
     log-uniform 8k-2M cells, 60% mixed AMG-PCG / 25% PCG+DIC / 15%
     PBiCGStab+DILU, tol 1e-8) submitted on its arrival schedule to the
@@ -250,16 +250,27 @@ def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 4):
         if dt > 0:
             time.sleep(dt)
         ids.append(srv.submit(r.system, r.method, rel_tol=1e-8, max_iter=2000))
-    lat, batched = [], 0
+    lat, batched, setup, solve_t, queue = [], 0, [], [], []
     for r, rid in zip(reqs, ids):
         _, info = srv.wait(rid, r.system.n)
         if not info["converged"]:
             raise RuntimeError(f"served request did not converge: {info}")
         lat.append(info["latencySeconds"])
+        setup.append(info["setupSeconds"])
+        solve_t.append(info["solveSeconds"])
+        queue.append(info["queueSeconds"])
         batched += info["batched"]
     span = time.perf_counter() - t0
     srv.close()
 
+    pct = lambda v, q: float(np.percentile(np.array(v), q))
+    out = {"requests": n_requests, "rate_per_s": 200.0,
+           "solves_per_s": n_requests / span, "p50_s": pct(lat, 50), "p99_s": pct(lat, 99),
+           "batched_requests": batched, "slots": max_slots,
+           "mean_queue_s": float(np.mean(queue)), "mean_setup_s": float(np.mean(setup)),
+           "mean_solve_s": float(np.mean(solve_t))}
+    if not compare_plain:
+        return out
     # the plain path: one request at a time, FP64 everywhere
     seq_lat = []
     t1 = time.perf_counter()
@@ -280,13 +291,10 @@ def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 4):
         A.close()
         seq_lat.append(time.perf_counter() - ts)
     seq_span = time.perf_counter() - t1
-    pct = lambda v, q: float(np.percentile(np.array(v), q))
-    return {"requests": n_requests, "rate_per_s": 200.0,
-            "solves_per_s": n_requests / span, "p50_s": pct(lat, 50), "p99_s": pct(lat, 99),
-            "batched_requests": batched, "slots": max_slots,
-            "one_at_a_time_fp64": {"solves_per_s": n_requests / seq_span,
-                                   "p50_s": pct(seq_lat, 50), "p99_s": pct(seq_lat, 99),
-                                   "latency": "solve time alone, no queueing"}}
+    out["one_at_a_time_fp64"] = {"solves_per_s": n_requests / seq_span,
+                                 "p50_s": pct(seq_lat, 50), "p99_s": pct(seq_lat, 99),
+                                 "latency": "solve time alone, no queueing"}
+    return out
 
 
 def kernels_case(args):
@@ -319,6 +327,8 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=3)
     ap.add_argument("--serve", type=int, default=0,
                     help="also serve this many requests of the c5 stream")
+    ap.add_argument("--serve-slots", type=int, default=4,
+                    help="concurrent large-request slots of the server")
     ap.add_argument("--kernels", action="store_true",
                     help="only time the finest-level kernels one launch at a time "
                          "(the small case for kernel profiles) and exit")
@@ -456,7 +466,7 @@ def main():
     serving = None
     if args.serve > 0 and rank == 0:
         try:
-            serving = serve_bench(args.serve, seed=rank)
+            serving = serve_bench(args.serve, seed=rank, max_slots=args.serve_slots)
         except Exception as e:  # reported in the line, never fatal
             serving = {"error": str(e)}
 

@@ -327,6 +327,13 @@ int unap_cuda_set_executor(int persistent);
  * previous setting.  No counterpart in the reference. */
 int unap_cuda_set_wave_pdl(int on);
 
+/* Grid of the per-wavefront Gauss-Seidel launches: 1 (default) one CTA per
+ * 256 rows of the wavefront, so every row's matrix data is loaded before the
+ * dependency wait; 0 a grid-stride loop over at most (SMs x 8) CTAs.
+ * Results are identical.  Returns the previous setting.  No counterpart in
+ * the reference. */
+int unap_cuda_set_wave_grid(int oneRowPerThread);
+
 /* Coarse-level tail of the AMG V-cycle (per-step executor), set for the FP64
  * (precision 0) or FP32 (precision 1) V-cycle: every level with at most
  * tailRows rows whose iterate fits in the cluster's shared memory, down to

@@ -77,11 +77,13 @@ def test_preconditioners_bit_exact(cuda, orc):
         A.close()
 
 
-@pytest.mark.parametrize("pdl", [True, False])
-def test_gauss_seidel_bit_exact(cuda, orc, pdl):
-    """Wavefront launches with and without programmatic dependent launch."""
+@pytest.mark.parametrize("pdl,row_grid", [(True, True), (False, True), (True, False)])
+def test_gauss_seidel_bit_exact(cuda, orc, pdl, row_grid):
+    """Wavefront launches with and without programmatic dependent launch, one
+    row per thread or a grid-stride loop."""
     torch = cuda
     old = capi.set_wave_pdl(pdl)
+    old_grid = capi.set_wave_grid(row_grid)
     try:
         for s in systems():
             A = capi.DeviceMatrix(s)
@@ -94,6 +96,7 @@ def test_gauss_seidel_bit_exact(cuda, orc, pdl):
             A.close()
     finally:
         capi.set_wave_pdl(old)
+        capi.set_wave_grid(old_grid)
 
 
 def _solution_close(x, x_ref):

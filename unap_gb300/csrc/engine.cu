@@ -222,7 +222,9 @@ Krylov::Krylov(Matrix& A_, Precond* P_, Method m) : A(A_), P(P_), method(m)
     }
     UNAP_CK(cudaMalloc((void**)&d_st, sizeof(KState)));
     UNAP_CK(cudaMallocHost((void**)&h_st, sizeof(KState)));
-    pool.init(S_NSITES, ex.maxBlocks, std::max(1, A.L->nWave) + 1, ex.s);
+    // partial buffers for one CTA per 256 rows (row kernels launch that many)
+    pool.init(S_NSITES, std::max(ex.maxBlocks, div_up(n, kBlock)), std::max(1, A.L->nWave) + 1,
+              ex.s);
     UNAP_CK(cudaEventCreate(&ev0));
     UNAP_CK(cudaEventCreate(&ev1));
 }

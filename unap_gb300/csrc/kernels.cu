@@ -69,9 +69,9 @@ void k_spmv(const Exec& ex, const Rows<T>& A, const T* x, T* y, const T* dotWith
     if (A.n <= 0) return;
     const T* dw = red.blockPart ? dotWith : nullptr;
     if (A.wide)
-        tick(), spmv_kernel<T, 16><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
+        tick(), spmv_kernel<T, 16><<<ex.rowGrid(A.n, red), kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
     else
-        tick(), spmv_kernel<T, 8><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
+        tick(), spmv_kernel<T, 8><<<ex.rowGrid(A.n, red), kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
 }
 
 template <class T, int CK>
@@ -95,9 +95,9 @@ void k_residual(const Exec& ex, const Rows<T>& A, const T* x, const T* b, T* r, 
 {
     if (A.n <= 0) return;
     if (A.wide)
-        tick(), residual_kernel<T, 16><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, b, r, red, g);
+        tick(), residual_kernel<T, 16><<<ex.rowGrid(A.n, red), kBlock, 0, ex.s>>>(A, x, b, r, red, g);
     else
-        tick(), residual_kernel<T, 8><<<ex.grid(A.n), kBlock, 0, ex.s>>>(A, x, b, r, red, g);
+        tick(), residual_kernel<T, 8><<<ex.rowGrid(A.n, red), kBlock, 0, ex.s>>>(A, x, b, r, red, g);
 }
 
 // --------------------------------------------------------------------------
@@ -161,6 +161,8 @@ __global__ void __launch_bounds__(kBlock) gs_kernel(Rows<T> A, T* x, const T* __
 
 static std::atomic<int> g_pdl{1};
 int set_wave_pdl(int on) { return g_pdl.exchange(on ? 1 : 0); }
+static std::atomic<int> g_rowGrid{1};
+int set_wave_grid(int oneRowPerThread) { return g_rowGrid.exchange(oneRowPerThread ? 1 : 0); }
 
 // one wavefront launch, with programmatic dependent launch when enabled
 template <class T, int CK>
@@ -168,7 +170,10 @@ static void launch_gs(const Exec& ex, const Rows<T>& A, T* x, const T* b, int r0
                       int skipUpper, Gate g)
 {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)ex.grid(r1 - r0));
+    // one row per thread (every row's matrix data is loaded before the
+    // dependency wait), or a grid-stride loop over at most maxBlocks CTAs
+    const long long need = div_up(r1 - r0, kBlock);
+    cfg.gridDim = dim3((unsigned)(g_rowGrid.load() ? std::max(1LL, need) : ex.grid(r1 - r0)));
     cfg.blockDim = dim3(kBlock);
     cfg.stream = ex.s;
     cudaLaunchAttribute at[1];
@@ -762,6 +767,7 @@ RSpec RedPool::site(int i, KState* st, int fin, int slot, int nSlots) const
     r.nSlots = nSlots;
     r.fin = fin;
     r.st = st;
+    r.maxBlocks = maxBlocks;
     return r;
 }
 

@@ -189,6 +189,7 @@ struct RSpec {
     int nSlots = 1;  // launches to combine when finalizing
     int fin = FIN_NONE;
     KState* st = nullptr;
+    int maxBlocks = 0;  // blockPart holds partials of at most this many CTAs
 };
 
 // Gate: skip the kernel when st->done (mask 1) or st->early (mask 2) is set.
@@ -220,6 +221,15 @@ struct Exec {
     {
         int g = div_up(n, kBlock);
         return g < 1 ? 1 : (g > maxBlocks ? maxBlocks : g);
+    }
+    // one row per thread; a reducing launch stays within its reduction
+    // site's partial buffer
+    int rowGrid(long long n, const RSpec& red) const
+    {
+        int g = div_up(n, kBlock);
+        if (g < 1) g = 1;
+        if (red.blockPart && g > red.maxBlocks) g = red.maxBlocks;
+        return g;
     }
 };
 
