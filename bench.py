@@ -327,7 +327,7 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=3)
     ap.add_argument("--serve", type=int, default=0,
                     help="also serve this many requests of the c5 stream")
-    ap.add_argument("--serve-slots", type=int, default=4,
+    ap.add_argument("--serve-slots", type=int, default=12,
                     help="concurrent large-request slots of the server")
     ap.add_argument("--kernels", action="store_true",
                     help="only time the finest-level kernels one launch at a time "

@@ -334,6 +334,13 @@ int unap_cuda_set_wave_pdl(int on);
  * the reference. */
 int unap_cuda_set_wave_grid(int oneRowPerThread);
 
+/* AMG V-cycle Gauss-Seidel sweeps on levels whose rows average more than 8
+ * entries read a row-packed copy of the level (a row's entries as 16-byte
+ * records, loaded before the dependency wait) when 1 (default), the SELL-32
+ * storage when 0.  Results are identical.  Returns the previous setting.
+ * No counterpart in the reference. */
+int unap_cuda_set_packed_sweeps(int on);
+
 /* Coarse-level tail of the AMG V-cycle (per-step executor), set for the FP64
  * (precision 0) or FP32 (precision 1) V-cycle: every level with at most
  * tailRows rows whose iterate fits in the cluster's shared memory, down to

@@ -93,6 +93,7 @@ SIGNATURES = {
     "unap_cuda_set_executor": (_c_int, [_c_int]),
     "unap_cuda_set_wave_pdl": (_c_int, [_c_int]),
     "unap_cuda_set_wave_grid": (_c_int, [_c_int]),
+    "unap_cuda_set_packed_sweeps": (_c_int, [_c_int]),
     "unap_cuda_set_tail_rows": (_c_int, [_c_int, _c_ll, _c_ll, ctypes.POINTER(_c_ll),
                                          ctypes.POINTER(_c_ll)]),
     "unap_cuda_tail_cluster_size": (_c_int, [_ip]),
@@ -273,6 +274,11 @@ def set_wave_pdl(on: bool) -> bool:
 def set_wave_grid(one_row_per_thread: bool) -> bool:
     """Wavefront kernel grids: one row per thread, or a capped grid-stride loop."""
     return bool(load().unap_cuda_set_wave_grid(1 if one_row_per_thread else 0))
+
+
+def set_packed_sweeps(on: bool) -> bool:
+    """V-cycle sweeps on long-row levels from the row-packed copy."""
+    return bool(load().unap_cuda_set_packed_sweeps(1 if on else 0))
 
 
 def set_tail_rows(tail_rows: int, single_rows: int, precision: int | None = None):

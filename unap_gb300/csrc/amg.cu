@@ -282,6 +282,19 @@ void AmgHierarchy::launch_tail(const Exec& ex, int t, Gate g)
 }
 
 template <class T>
+void AmgHierarchy::sweep(const Exec& ex, int k, const Level& Lk, const Rows<T>& Rk, T* x,
+                         const T* b, bool backward, bool xIsZero, Gate g)
+{
+    const PackedRows& P = lv[(size_t)k].pack;
+    // the row-packed form on levels whose rows are long (more than 8
+    // entries on average), where the SELL chunks would chain two loads
+    if (P.rec.p && packed_sweeps() && Rk.wide)
+        gs_sweep_packed<T>(ex, Lk, P, Rk.diag, x, b, backward, xIsZero, g);
+    else
+        gs_sweep<T>(ex, Lk, Rk, x, b, backward, xIsZero, g);
+}
+
+template <class T>
 void AmgHierarchy::vcycle_level(const Exec& ex, int k, Gate g)
 {
     const int L = nLevels() - 1;
@@ -301,7 +314,7 @@ void AmgHierarchy::vcycle_level(const Exec& ex, int k, Gate g)
     const Level& Lk = *lv[(size_t)k].L;
     Rows<T> Rk = rowsT<T>(Lk);
     if (params.nPre > 0) {
-        for (int s = 0; s < params.nPre; ++s) gs_sweep<T>(ex, Lk, Rk, x, b, false, s == 0, g);
+        for (int s = 0; s < params.nPre; ++s) sweep<T>(ex, k, Lk, Rk, x, b, false, s == 0, g);
     } else {
         k_fill<T>(ex, Lk.n, x, T(0));
     }
@@ -311,7 +324,7 @@ void AmgHierarchy::vcycle_level(const Exec& ex, int k, Gate g)
     k_restrict<T>(ex, C.n, C.childStart.p, C.child.p, r, B<T>(k + 1), g);
     vcycle_level<T>(ex, k + 1, g);
     k_prolong_add<T>(ex, Lk.n, C.cmap.p, X<T>(k + 1), x, g);
-    for (int s = 0; s < params.nPost; ++s) gs_sweep<T>(ex, Lk, Rk, x, b, true, false, g);
+    for (int s = 0; s < params.nPost; ++s) sweep<T>(ex, k, Lk, Rk, x, b, true, false, g);
     if (profOut) UNAP_CK(cudaEventRecordWithFlags((*profOut)[(size_t)k], ex.s, cudaEventRecordExternal));
 }
 

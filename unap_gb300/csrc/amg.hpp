@@ -84,6 +84,9 @@ private:
     void vcycle_level(const Exec& ex, int k, Gate g);
     template <class T>
     void launch_tail(const Exec& ex, int t, Gate g);
+    template <class T>
+    void sweep(const Exec& ex, int k, const Level& Lk, const Rows<T>& Rk, T* x, const T* b,
+               bool backward, bool xIsZero, Gate g);
     int curTail = -1;
     std::vector<cudaEvent_t>* profIn = nullptr;   // per-level events (profiling)
     std::vector<cudaEvent_t>* profOut = nullptr;

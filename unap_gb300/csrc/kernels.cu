@@ -161,6 +161,7 @@ __global__ void __launch_bounds__(kBlock) gs_kernel(Rows<T> A, T* x, const T* __
 
 static std::atomic<int> g_pdl{1};
 int set_wave_pdl(int on) { return g_pdl.exchange(on ? 1 : 0); }
+bool wave_pdl() { return g_pdl.load() != 0; }
 static std::atomic<int> g_rowGrid{1};
 int set_wave_grid(int oneRowPerThread) { return g_rowGrid.exchange(oneRowPerThread ? 1 : 0); }
 

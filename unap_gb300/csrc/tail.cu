@@ -23,6 +23,8 @@ namespace {
 // hierarchy: per-wavefront launches with programmatic dependent launch beat
 // the cluster tail on FP32 levels above ~30k rows; FP64 levels are slower
 // per launch, so the tail pays off from larger levels on
+std::atomic<int> g_packedSweeps{1};
+
 std::atomic<long long> g_tailRows[2] = {{1ll << 21}, {1ll << 15}};
 std::atomic<long long> g_singleRows[2] = {{8192}, {1ll << 30}};
 
@@ -577,6 +579,9 @@ void set_tail_rows(int precision, long long tailRows, long long singleRows, long
     if (oldSingle) *oldSingle = s;
 }
 
+int set_packed_sweeps(int on) { return g_packedSweeps.exchange(on ? 1 : 0); }
+bool packed_sweeps() { return g_packedSweeps.load() != 0; }
+
 long long tail_rows(int precision) { return g_tailRows[precision ? 1 : 0].load(); }
 long long single_rows(int precision) { return g_singleRows[precision ? 1 : 0].load(); }
 
@@ -659,6 +664,103 @@ void pack_rows(const Rows<T>& A, PackedRows& out, cudaStream_t s)
     }
     UNAP_CK(cudaStreamSynchronize(s));
 }
+
+namespace {
+
+template <class T, int KW>
+__global__ void __launch_bounds__(kBlock) gs_packed_kernel(const int2* __restrict__ meta,
+                                                           const int4* __restrict__ rec,
+                                                           const T* __restrict__ diag, T* x,
+                                                           const T* __restrict__ b, int r0, int r1,
+                                                           int skipUpper, Gate g)
+{
+    constexpr int EPR = Pk<T>::EPR;
+    constexpr int R = KW / EPR;
+    // the next wavefront's kernel may launch now; before the wait this
+    // kernel reads only data no kernel of the sweep writes
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const int r = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+    int start = 0, info = 0;
+    T d = T(1), bb = T(0);
+    int4 q[R];
+    if (r < r1) {
+        const int2 m = ldg(meta + r);
+        start = m.x;
+        info = m.y;
+        d = ldg(diag + r);
+        bb = ldg(b + r);
+        const int len = info & 0xffff;
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+            if (k * EPR < len) q[k] = ldg(rec + start + k);
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (gate_closed(g) || r >= r1) return;
+    const int jEnd = skipUpper ? (info >> 16) : (info & 0xffff);
+    T xv[KW];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+#pragma unroll
+        for (int h = 0; h < EPR; ++h) {
+            int col;
+            T v;
+            Pk<T>::entry(q[k], h, col, v);
+            xv[k * EPR + h] = k * EPR + h < jEnd ? x[col] : T(0);
+        }
+    }
+    T acc = bb;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+#pragma unroll
+        for (int h = 0; h < EPR; ++h) {
+            if (k * EPR + h < jEnd) {
+                int col;
+                T v;
+                Pk<T>::entry(q[k], h, col, v);
+                acc -= v * xv[k * EPR + h];
+            }
+        }
+    }
+    for (int j = KW; j < jEnd; ++j) {
+        int col;
+        T v;
+        Pk<T>::entry(ldg(rec + start + j / EPR), j % EPR, col, v);
+        acc -= v * x[col];
+    }
+    x[r] = acc / d;
+}
+
+}  // namespace
+
+template <class T>
+void gs_sweep_packed(const Exec& ex, const Level& L, const PackedRows& P, const T* diag, T* x,
+                     const T* b, bool backward, bool xIsZero, Gate g)
+{
+    constexpr int KW = sizeof(T) == 4 ? 24 : 12;
+    const int W = L.nWave;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    for (int k = 0; k < W; ++k) {
+        const int w = backward ? W - 1 - k : k;
+        const int r0 = L.waveStart[(size_t)w], r1 = L.waveStart[(size_t)w + 1];
+        if (r1 <= r0) continue;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)div_up(r1 - r0, kBlock));
+        cfg.blockDim = dim3(kBlock);
+        cfg.stream = ex.s;
+        cfg.attrs = at;
+        cfg.numAttrs = wave_pdl() ? 1 : 0;
+        if (!capturing()) count_launches(1);
+        UNAP_CK(cudaLaunchKernelEx(&cfg, gs_packed_kernel<T, KW>, P.meta.p, P.rec.p, diag, x, b,
+                                   r0, r1, (xIsZero && !backward) ? 1 : 0, g));
+    }
+}
+
+template void gs_sweep_packed<float>(const Exec&, const Level&, const PackedRows&, const float*,
+                                     float*, const float*, bool, bool, Gate);
+template void gs_sweep_packed<double>(const Exec&, const Level&, const PackedRows&, const double*,
+                                      double*, const double*, bool, bool, Gate);
 
 template void pack_rows<float>(const Rows<float>&, PackedRows&, cudaStream_t);
 template void pack_rows<double>(const Rows<double>&, PackedRows&, cudaStream_t);

@@ -68,6 +68,20 @@ struct PackedRows {
 template <class T>
 void pack_rows(const Rows<T>& A, PackedRows& out, cudaStream_t s);
 
+// Gauss-Seidel sweep of a level, one launch per wavefront like gs_sweep,
+// reading the row-packed copy: a thread loads its row's first 24 (FP32) or
+// 12 (FP64) entries as 16-byte records before the dependency wait of the
+// programmatic dependent launch, so after it only the x gathers remain.
+// Same arithmetic and results as gs_sweep.
+// 1 (default): AMG V-cycle sweeps on levels with long rows use
+// gs_sweep_packed; 0: the SELL-32 kernel.  Returns the previous value.
+int set_packed_sweeps(int on);
+bool packed_sweeps();
+
+template <class T>
+void gs_sweep_packed(const Exec& ex, const Level& L, const PackedRows& P, const T* diag, T* x,
+                     const T* b, bool backward, bool xIsZero, Gate g);
+
 struct TailArgs {
     TailLevel lv[kTailMaxLevels];
     int nLv = 0, nPre = 2, nPost = 2;
