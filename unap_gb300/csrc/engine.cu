@@ -532,35 +532,111 @@ SolveStats Krylov::solveHost(double* xh, const double* bh)
 // bits).
 bool dense_spd_inverse(int n, const std::vector<double>& A, std::vector<double>& inv)
 {
+    // Cholesky A = L L^T, then Li = L^-1, then inv = Li^T Li.  Every element
+    // is a sum in ascending k, the order the oracle uses; the loops run four
+    // independent sums side by side over contiguous rows for speed.
     const size_t N = (size_t)n;
-    std::vector<double> L(N * N, 0.0), Li(N * N, 0.0);
+    std::vector<double> L(N * N, 0.0), LiT(N * N, 0.0);  // LiT[j*N + k] = Li[k][j]
     inv.assign(N * N, 0.0);
     for (int j = 0; j < n; ++j) {
+        const double* Lj = &L[(size_t)j * N];
         double s = A[(size_t)j * N + j];
-        for (int k = 0; k < j; ++k) s -= L[(size_t)j * N + k] * L[(size_t)j * N + k];
+        for (int k = 0; k < j; ++k) s -= Lj[k] * Lj[k];
         if (!(s > 0.0)) return false;
-        double djj = std::sqrt(s);
+        const double djj = std::sqrt(s);
         L[(size_t)j * N + j] = djj;
-        for (int i = j + 1; i < n; ++i) {
+        int i = j + 1;
+        for (; i + 3 < n; i += 4) {
+            const double* a0 = &L[(size_t)i * N];
+            const double* a1 = a0 + N;
+            const double* a2 = a1 + N;
+            const double* a3 = a2 + N;
+            double t0 = A[(size_t)i * N + j], t1 = A[(size_t)(i + 1) * N + j];
+            double t2 = A[(size_t)(i + 2) * N + j], t3 = A[(size_t)(i + 3) * N + j];
+            for (int k = 0; k < j; ++k) {
+                const double l = Lj[k];
+                t0 -= a0[k] * l;
+                t1 -= a1[k] * l;
+                t2 -= a2[k] * l;
+                t3 -= a3[k] * l;
+            }
+            L[(size_t)i * N + j] = t0 / djj;
+            L[(size_t)(i + 1) * N + j] = t1 / djj;
+            L[(size_t)(i + 2) * N + j] = t2 / djj;
+            L[(size_t)(i + 3) * N + j] = t3 / djj;
+        }
+        for (; i < n; ++i) {
+            const double* ai = &L[(size_t)i * N];
             double t = A[(size_t)i * N + j];
-            const double* Li_ = &L[(size_t)i * N];
-            const double* Lj_ = &L[(size_t)j * N];
-            for (int k = 0; k < j; ++k) t -= Li_[k] * Lj_[k];
+            for (int k = 0; k < j; ++k) t -= ai[k] * Lj[k];
             L[(size_t)i * N + j] = t / djj;
         }
     }
-    for (int j = 0; j < n; ++j) {
-        Li[(size_t)j * N + j] = 1.0 / L[(size_t)j * N + j];
-        for (int i = j + 1; i < n; ++i) {
+    // Li row by row: Li[i][j] = -(sum_{k=j}^{i-1} L[i][k] Li[k][j]) / L[i][i]
+    for (int i = 0; i < n; ++i) {
+        const double* Lr = &L[(size_t)i * N];
+        const double lii = Lr[i];
+        LiT[(size_t)i * N + i] = 1.0 / lii;
+        int j = 0;
+        for (; j + 3 < i; j += 4) {
+            const double* c0 = &LiT[(size_t)j * N];
+            const double* c1 = c0 + N;
+            const double* c2 = c1 + N;
+            const double* c3 = c2 + N;
+            double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+            // sums start at k = j, j+1, j+2, j+3 respectively
+            t0 += Lr[j] * c0[j];
+            t0 += Lr[j + 1] * c0[j + 1];
+            t1 += Lr[j + 1] * c1[j + 1];
+            t0 += Lr[j + 2] * c0[j + 2];
+            t1 += Lr[j + 2] * c1[j + 2];
+            t2 += Lr[j + 2] * c2[j + 2];
+            for (int k = j + 3; k < i; ++k) {
+                const double l = Lr[k];
+                t0 += l * c0[k];
+                t1 += l * c1[k];
+                t2 += l * c2[k];
+                t3 += l * c3[k];
+            }
+            LiT[(size_t)j * N + i] = -t0 / lii;
+            LiT[(size_t)(j + 1) * N + i] = -t1 / lii;
+            LiT[(size_t)(j + 2) * N + i] = -t2 / lii;
+            LiT[(size_t)(j + 3) * N + i] = -t3 / lii;
+        }
+        for (; j < i; ++j) {
+            const double* c = &LiT[(size_t)j * N];
             double t = 0.0;
-            for (int k = j; k < i; ++k) t += L[(size_t)i * N + k] * Li[(size_t)k * N + j];
-            Li[(size_t)i * N + j] = -t / L[(size_t)i * N + i];
+            for (int k = j; k < i; ++k) t += Lr[k] * c[k];
+            LiT[(size_t)j * N + i] = -t / lii;
         }
     }
+    // inv[i][j] = sum_{k=i}^{n-1} Li[k][i] Li[k][j], j <= i
     for (int i = 0; i < n; ++i) {
-        for (int j = 0; j <= i; ++j) {
+        const double* ci = &LiT[(size_t)i * N];
+        int j = 0;
+        for (; j + 3 <= i; j += 4) {
+            const double* c0 = &LiT[(size_t)j * N];
+            const double* c1 = c0 + N;
+            const double* c2 = c1 + N;
+            const double* c3 = c2 + N;
+            double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+            for (int k = i; k < n; ++k) {
+                const double a = ci[k];
+                t0 += a * c0[k];
+                t1 += a * c1[k];
+                t2 += a * c2[k];
+                t3 += a * c3[k];
+            }
+            const double t[4] = {t0, t1, t2, t3};
+            for (int q = 0; q < 4; ++q) {
+                inv[(size_t)i * N + j + q] = t[q];
+                inv[(size_t)(j + q) * N + i] = t[q];
+            }
+        }
+        for (; j <= i; ++j) {
+            const double* cj = &LiT[(size_t)j * N];
             double t = 0.0;
-            for (int k = i; k < n; ++k) t += Li[(size_t)k * N + i] * Li[(size_t)k * N + j];
+            for (int k = i; k < n; ++k) t += ci[k] * cj[k];
             inv[(size_t)i * N + j] = t;
             inv[(size_t)j * N + i] = t;
         }

@@ -132,11 +132,20 @@ std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key
             rank = *key;
         else
             rank = bfs_rank(n, loStart, loList, ownStart, ownList, l, u);
-        // cells in key order (keys may repeat: stable on cell index)
+        // cells in key order (keys may repeat: stable on cell index), by a
+        // counting sort over the key range
+        int maxKey = 0;
+        for (int c = 0; c < n; ++c) {
+            if (rank[(size_t)c] < 0) throw std::invalid_argument("negative locality key");
+            maxKey = std::max(maxKey, rank[(size_t)c]);
+        }
         std::vector<int> byKey((size_t)n);
-        std::iota(byKey.begin(), byKey.end(), 0);
-        std::stable_sort(byKey.begin(), byKey.end(),
-                         [&](int a, int b) { return rank[(size_t)a] < rank[(size_t)b]; });
+        {
+            std::vector<int> cnt((size_t)maxKey + 2, 0);
+            for (int c = 0; c < n; ++c) cnt[(size_t)rank[(size_t)c] + 1]++;
+            for (int k = 0; k <= maxKey; ++k) cnt[(size_t)k + 1] += cnt[(size_t)k];
+            for (int c = 0; c < n; ++c) byKey[(size_t)cnt[(size_t)rank[(size_t)c]]++] = c;
+        }
         L->waveStart.assign((size_t)nWave + 1, 0);
         for (int c = 0; c < n; ++c) L->waveStart[(size_t)wave[(size_t)c] + 1]++;
         for (int w = 0; w < nWave; ++w) L->waveStart[(size_t)w + 1] += L->waveStart[(size_t)w];
