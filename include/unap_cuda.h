@@ -336,10 +336,11 @@ int unap_cuda_set_wave_grid(int oneRowPerThread);
 
 /* AMG V-cycle Gauss-Seidel sweeps on levels whose rows average more than 8
  * entries read a row-packed copy of the level (a row's entries as 16-byte
- * records, loaded before the dependency wait) when 1 (default), the SELL-32
- * storage when 0.  Results are identical.  Returns the previous setting.
- * No counterpart in the reference. */
-int unap_cuda_set_packed_sweeps(int on);
+ * records, loaded before the dependency wait): mode 1 (default) holds the
+ * first 24 (FP32) / 12 (FP64) entries in registers, mode 2 the first 16 / 8;
+ * mode 0 reads the SELL-32 storage.  Results are identical.  Returns the
+ * previous setting.  No counterpart in the reference. */
+int unap_cuda_set_packed_sweeps(int mode);
 
 /* Coarse-level tail of the AMG V-cycle (per-step executor), set for the FP64
  * (precision 0) or FP32 (precision 1) V-cycle: every level with at most

@@ -276,9 +276,10 @@ def set_wave_grid(one_row_per_thread: bool) -> bool:
     return bool(load().unap_cuda_set_wave_grid(1 if one_row_per_thread else 0))
 
 
-def set_packed_sweeps(on: bool) -> bool:
-    """V-cycle sweeps on long-row levels from the row-packed copy."""
-    return bool(load().unap_cuda_set_packed_sweeps(1 if on else 0))
+def set_packed_sweeps(mode) -> int:
+    """V-cycle sweeps on long-row levels from the row-packed copy: 1 (or True)
+    24/12 entries in registers, 2 16/8, 0 (or False) SELL-32 rows."""
+    return int(load().unap_cuda_set_packed_sweeps(int(mode)))
 
 
 def set_tail_rows(tail_rows: int, single_rows: int, precision: int | None = None):

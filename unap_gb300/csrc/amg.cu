@@ -288,7 +288,7 @@ void AmgHierarchy::sweep(const Exec& ex, int k, const Level& Lk, const Rows<T>& 
     const PackedRows& P = lv[(size_t)k].pack;
     // the row-packed form on levels whose rows are long (more than 8
     // entries on average), where the SELL chunks would chain two loads
-    if (P.rec.p && packed_sweeps() && Rk.wide)
+    if (P.rec.p && packed_sweeps() != 0 && Rk.wide)
         gs_sweep_packed<T>(ex, Lk, P, Rk.diag, x, b, backward, xIsZero, g);
     else
         gs_sweep<T>(ex, Lk, Rk, x, b, backward, xIsZero, g);

@@ -194,7 +194,7 @@ int unap_cuda_set_wave_pdl(int on) { return set_wave_pdl(on); }
 
 int unap_cuda_set_wave_grid(int oneRowPerThread) { return set_wave_grid(oneRowPerThread); }
 
-int unap_cuda_set_packed_sweeps(int on) { return set_packed_sweeps(on); }
+int unap_cuda_set_packed_sweeps(int mode) { return set_packed_sweeps(mode); }
 
 int unap_cuda_set_tail_rows(int precision, long long tailRows, long long singleRows,
                             long long* oldTailRows, long long* oldSingleRows)

@@ -579,8 +579,8 @@ void set_tail_rows(int precision, long long tailRows, long long singleRows, long
     if (oldSingle) *oldSingle = s;
 }
 
-int set_packed_sweeps(int on) { return g_packedSweeps.exchange(on ? 1 : 0); }
-bool packed_sweeps() { return g_packedSweeps.load() != 0; }
+int set_packed_sweeps(int mode) { return g_packedSweeps.exchange(mode < 0 || mode > 2 ? 1 : mode); }
+int packed_sweeps() { return g_packedSweeps.load(); }
 
 long long tail_rows(int precision) { return g_tailRows[precision ? 1 : 0].load(); }
 long long single_rows(int precision) { return g_singleRows[precision ? 1 : 0].load(); }
@@ -736,7 +736,7 @@ template <class T>
 void gs_sweep_packed(const Exec& ex, const Level& L, const PackedRows& P, const T* diag, T* x,
                      const T* b, bool backward, bool xIsZero, Gate g)
 {
-    constexpr int KW = sizeof(T) == 4 ? 24 : 12;
+    const bool narrow = packed_sweeps() == 2;
     const int W = L.nWave;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -752,8 +752,13 @@ void gs_sweep_packed(const Exec& ex, const Level& L, const PackedRows& P, const 
         cfg.attrs = at;
         cfg.numAttrs = wave_pdl() ? 1 : 0;
         if (!capturing()) count_launches(1);
-        UNAP_CK(cudaLaunchKernelEx(&cfg, gs_packed_kernel<T, KW>, P.meta.p, P.rec.p, diag, x, b,
-                                   r0, r1, (xIsZero && !backward) ? 1 : 0, g));
+        const int skip = (xIsZero && !backward) ? 1 : 0;
+        if (narrow)
+            UNAP_CK(cudaLaunchKernelEx(&cfg, gs_packed_kernel<T, sizeof(T) == 4 ? 16 : 8>, P.meta.p,
+                                       P.rec.p, diag, x, b, r0, r1, skip, g));
+        else
+            UNAP_CK(cudaLaunchKernelEx(&cfg, gs_packed_kernel<T, sizeof(T) == 4 ? 24 : 12>,
+                                       P.meta.p, P.rec.p, diag, x, b, r0, r1, skip, g));
     }
 }
 

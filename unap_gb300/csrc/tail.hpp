@@ -32,7 +32,7 @@ constexpr int kTailThreads = 256;
 constexpr int kTailMaxWaves = 4096;  // wave starts of all tail levels, staged in shared memory
 constexpr int kTailMaxCoarsest = 4096;
 constexpr int kTailMaxCluster = 16;
-constexpr int kTailPackRows = 1 << 22;  // levels up to this size get a row-packed copy
+constexpr int kTailPackRows = 1 << 24;  // levels up to this size get a row-packed copy
 
 // One smoothed level of the tail (pointers to T = float or double data).
 struct TailLevel {
@@ -74,9 +74,10 @@ void pack_rows(const Rows<T>& A, PackedRows& out, cudaStream_t s);
 // programmatic dependent launch, so after it only the x gathers remain.
 // Same arithmetic and results as gs_sweep.
 // 1 (default): AMG V-cycle sweeps on levels with long rows use
-// gs_sweep_packed; 0: the SELL-32 kernel.  Returns the previous value.
-int set_packed_sweeps(int on);
-bool packed_sweeps();
+// gs_sweep_packed holding 24 (FP32) / 12 (FP64) entries in registers; 2: the
+// same with 16 / 8; 0: the SELL-32 kernel.  Returns the previous value.
+int set_packed_sweeps(int mode);
+int packed_sweeps();
 
 template <class T>
 void gs_sweep_packed(const Exec& ex, const Level& L, const PackedRows& P, const T* diag, T* x,
