@@ -337,9 +337,11 @@ int unap_cuda_set_wave_grid(int oneRowPerThread);
 /* AMG V-cycle Gauss-Seidel sweeps on levels whose rows average more than 8
  * entries read a row-packed copy of the level (a row's entries as 16-byte
  * records, loaded before the dependency wait): mode 1 (default) holds the
- * first 24 (FP32) / 12 (FP64) entries in registers, mode 2 the first 16 / 8;
- * mode 0 reads the SELL-32 storage.  Results are identical.  Returns the
- * previous setting.  No counterpart in the reference. */
+ * first 16 (FP32) / 8 (FP64) entries in registers on levels averaging under
+ * 12.5 entries per row and 24 / 12 above; mode 2 always 16 / 8, mode 3
+ * always 24 / 12; mode 0 reads the SELL-32 storage.  Results are
+ * identical.  Returns the previous setting.  No counterpart in the
+ * reference. */
 int unap_cuda_set_packed_sweeps(int mode);
 
 /* Coarse-level tail of the AMG V-cycle (per-step executor), set for the FP64
@@ -350,7 +352,7 @@ int unap_cuda_set_packed_sweeps(int mode);
  * levels with at most singleRows rows run on the cluster's first CTA alone.
  * tailRows = 0 launches one kernel per wavefront on every level.  The
  * V-cycle result is bit-identical either way.  Defaults: FP64 2097152 and
- * 8192, FP32 32768 and 2^30; the previous values are returned through the
+ * 8192, FP32 0 (off) and 2^30; the previous values are returned through the
  * (nullable) pointers.  Applies to V-cycles launched after the call, CUDA
  * graphs captured before keep their launches.  No counterpart in the
  * reference. */

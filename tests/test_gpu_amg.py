@@ -105,7 +105,7 @@ def test_amg_pcg_same_bits_in_every_tail_mode(cuda, precision):
     s = W.lognormal(24, 20, 18, seed=11, permute=True)
     A = capi.DeviceMatrix(s)
     b = dev(torch, s.b)
-    modes = ["per-wavefront", "sell-sweeps", "packed-narrow"] + (
+    modes = ["per-wavefront", "sell-sweeps", "packed-narrow", "packed-wide"] + (
         ["cluster", "one-cta", "split"] if capi.tail_cluster_size() > 0 else [])
     results = {}
     old = capi.set_tail_rows(*TAIL_MODES["per-wavefront"])
@@ -113,7 +113,8 @@ def test_amg_pcg_same_bits_in_every_tail_mode(cuda, precision):
         for m in modes:
             # "sell-sweeps" / "packed-narrow": per-wavefront launches reading
             # the SELL-32 rows, or the row-packed copy with a 16/8-entry window
-            capi.set_packed_sweeps({"sell-sweeps": 0, "packed-narrow": 2}.get(m, 1))
+            capi.set_packed_sweeps({"sell-sweeps": 0, "packed-narrow": 2,
+                                    "packed-wide": 3}.get(m, 1))
             capi.set_tail_rows(*TAIL_MODES[m if m in TAIL_MODES else "per-wavefront"])
             G = capi.DeviceAmg(A, n_coarsest=60, precision=precision, rel_tol=1e-10)
             x = torch.zeros(s.n, dtype=torch.float64, device="cuda")

@@ -278,7 +278,8 @@ def set_wave_grid(one_row_per_thread: bool) -> bool:
 
 def set_packed_sweeps(mode) -> int:
     """V-cycle sweeps on long-row levels from the row-packed copy: 1 (or True)
-    24/12 entries in registers, 2 16/8, 0 (or False) SELL-32 rows."""
+    register window by mean row length, 2 always 16/8 entries, 3 always
+    24/12, 0 (or False) SELL-32 rows."""
     return int(load().unap_cuda_set_packed_sweeps(int(mode)))
 
 

@@ -288,8 +288,12 @@ void AmgHierarchy::sweep(const Exec& ex, int k, const Level& Lk, const Rows<T>& 
     const PackedRows& P = lv[(size_t)k].pack;
     // the row-packed form on levels whose rows are long (more than 8
     // entries on average), where the SELL chunks would chain two loads
-    if (P.rec.p && packed_sweeps() != 0 && Rk.wide)
-        gs_sweep_packed<T>(ex, Lk, P, Rk.diag, x, b, backward, xIsZero, g);
+    const int mode = packed_sweeps();
+    if (P.rec.p && mode != 0 && Rk.wide) {
+        // register window by mean row length (measured per level on 256^3)
+        const bool wide = mode == 3 || (mode == 1 && 2.0 * Lk.nf > 12.5 * Lk.n);
+        gs_sweep_packed<T>(ex, Lk, P, Rk.diag, x, b, backward, xIsZero, wide, g);
+    }
     else
         gs_sweep<T>(ex, Lk, Rk, x, b, backward, xIsZero, g);
 }

@@ -20,12 +20,12 @@ namespace unapgpu {
 namespace {
 
 // per V-cycle precision (0 FP64, 1 FP32), measured on the 256^3 log-normal
-// hierarchy: per-wavefront launches with programmatic dependent launch beat
-// the cluster tail on FP32 levels above ~30k rows; FP64 levels are slower
-// per launch, so the tail pays off from larger levels on
+// hierarchy: FP32 per-wavefront launches of the row-packed sweep (with
+// programmatic dependent launch) beat the cluster tail on every level, so it
+// is off; FP64 launches are slower and the tail still wins from ~100k rows
 std::atomic<int> g_packedSweeps{1};
 
-std::atomic<long long> g_tailRows[2] = {{1ll << 21}, {1ll << 15}};
+std::atomic<long long> g_tailRows[2] = {{1ll << 21}, {0}};
 std::atomic<long long> g_singleRows[2] = {{8192}, {1ll << 30}};
 
 constexpr int kStaticSmem =
@@ -579,7 +579,7 @@ void set_tail_rows(int precision, long long tailRows, long long singleRows, long
     if (oldSingle) *oldSingle = s;
 }
 
-int set_packed_sweeps(int mode) { return g_packedSweeps.exchange(mode < 0 || mode > 2 ? 1 : mode); }
+int set_packed_sweeps(int mode) { return g_packedSweeps.exchange(mode < 0 || mode > 3 ? 1 : mode); }
 int packed_sweeps() { return g_packedSweeps.load(); }
 
 long long tail_rows(int precision) { return g_tailRows[precision ? 1 : 0].load(); }
@@ -734,9 +734,9 @@ __global__ void __launch_bounds__(kBlock) gs_packed_kernel(const int2* __restric
 
 template <class T>
 void gs_sweep_packed(const Exec& ex, const Level& L, const PackedRows& P, const T* diag, T* x,
-                     const T* b, bool backward, bool xIsZero, Gate g)
+                     const T* b, bool backward, bool xIsZero, bool wide, Gate g)
 {
-    const bool narrow = packed_sweeps() == 2;
+    const bool narrow = !wide;
     const int W = L.nWave;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -763,9 +763,9 @@ void gs_sweep_packed(const Exec& ex, const Level& L, const PackedRows& P, const 
 }
 
 template void gs_sweep_packed<float>(const Exec&, const Level&, const PackedRows&, const float*,
-                                     float*, const float*, bool, bool, Gate);
+                                     float*, const float*, bool, bool, bool, Gate);
 template void gs_sweep_packed<double>(const Exec&, const Level&, const PackedRows&, const double*,
-                                      double*, const double*, bool, bool, Gate);
+                                      double*, const double*, bool, bool, bool, Gate);
 
 template void pack_rows<float>(const Rows<float>&, PackedRows&, cudaStream_t);
 template void pack_rows<double>(const Rows<double>&, PackedRows&, cudaStream_t);

@@ -73,15 +73,16 @@ void pack_rows(const Rows<T>& A, PackedRows& out, cudaStream_t s);
 // 12 (FP64) entries as 16-byte records before the dependency wait of the
 // programmatic dependent launch, so after it only the x gathers remain.
 // Same arithmetic and results as gs_sweep.
-// 1 (default): AMG V-cycle sweeps on levels with long rows use
-// gs_sweep_packed holding 24 (FP32) / 12 (FP64) entries in registers; 2: the
-// same with 16 / 8; 0: the SELL-32 kernel.  Returns the previous value.
+// AMG V-cycle sweeps on levels with long rows: 1 (default) gs_sweep_packed
+// with the register window chosen by the level's mean row length (16 / 8
+// entries below 12.5 entries per row, 24 / 12 above); 2 always 16 / 8; 3
+// always 24 / 12; 0 the SELL-32 kernel.  Returns the previous value.
 int set_packed_sweeps(int mode);
 int packed_sweeps();
 
 template <class T>
 void gs_sweep_packed(const Exec& ex, const Level& L, const PackedRows& P, const T* diag, T* x,
-                     const T* b, bool backward, bool xIsZero, Gate g);
+                     const T* b, bool backward, bool xIsZero, bool wide, Gate g);
 
 struct TailArgs {
     TailLevel lv[kTailMaxLevels];
