@@ -315,6 +315,64 @@ def kernels_case(args):
     A.close()
 
 
+def textio_case(args):
+    """Host text I/O of the workload's matrix in the reference's LDU dump
+    format: print it, read it back (both through the C ABI, from a pool of
+    host threads), and, where the reference build oracle/_ref loads (the x86
+    host it was compiled on), the reference's own reader and printer on the
+    same file.  No GPU work."""
+    import shutil
+    import tempfile
+    from unap_gb300 import capi
+    from unap_gb300 import workloads as W
+
+    s = W.config(args.workload, args.scale, seed=0)
+    h0 = capi.ldumatrixcreat(s)
+    d = tempfile.mkdtemp(prefix="unap_textio_")
+    out = {"mode": "textio", "workload": args.workload, "scale": args.scale, "cells": s.n,
+           "faces": s.nf, "threads": os.cpu_count()}
+    try:
+        t = time.perf_counter()
+        f = capi.print_ldu_matrix(h0, os.path.join(d, "A"))
+        out["print_s"] = time.perf_counter() - t
+        out["file_mb"] = os.path.getsize(f) / 1e6
+        t = time.perf_counter()
+        h = capi.read_ldu_matrix(f)
+        out["read_s"] = time.perf_counter() - t
+        m = capi.handle_ldu(h)
+        out["read_matches_print"] = bool(np.array_equal(m["upper_addr"], s.upper_addr))
+        capi.sw_matrix_destroy(h)
+        ref = None
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "tests"))
+            from oracle_lib import Oracle, ref_available
+            ref = Oracle("ref").lib if ref_available() else None
+        except OSError as e:  # an x86 build on another host
+            out["reference"] = f"unavailable: {e}"
+        if ref is not None:
+            import ctypes
+            ref.ref_read_ldu.restype = ctypes.c_void_p
+            ref.ref_read_ldu.argtypes = [ctypes.c_char_p]
+            ref.ref_print_ldu.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+            ref.ref_ldu_destroy.argtypes = [ctypes.c_void_p]
+            t = time.perf_counter()
+            A = ref.ref_read_ldu(os.fsencode(f))
+            rr = time.perf_counter() - t
+            t = time.perf_counter()
+            ref.ref_print_ldu(A, os.fsencode(os.path.join(d, "B")))
+            rp = time.perf_counter() - t
+            ref.ref_ldu_destroy(A)
+            same = open(f, "rb").read() == open(os.path.join(d, "B_0.txt"), "rb").read()
+            out["reference"] = {"read_s": rr, "print_s": rp, "cores": 1,
+                                "files_byte_identical": same}
+        elif "reference" not in out:
+            out["reference"] = "unavailable: oracle/_ref not built on this host"
+    finally:
+        capi.sw_matrix_destroy(h0)
+        shutil.rmtree(d, ignore_errors=True)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -333,7 +391,12 @@ def main():
                     help="only time the finest-level kernels one launch at a time "
                          "(the small case for kernel profiles) and exit")
     ap.add_argument("--reps", type=int, default=5, help="repetitions for --kernels")
+    ap.add_argument("--textio", action="store_true",
+                    help="only time the LDU text dump printer and reader (host) and exit")
     args = ap.parse_args()
+    if args.textio:
+        textio_case(args)
+        return
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
     if args.kernels:

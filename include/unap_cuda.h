@@ -370,6 +370,43 @@ int unap_cuda_tail_cluster_size(int* clusterSize);
  * (*recovered = 1).  Nothing faults and nothing waits without a bound. */
 int unap_cuda_selftest_barrier_timeout(int* timedOut, int* recovered);
 
+/* ---- Text dumps in the reference's on-disk formats (host only; no GPU
+ * work).  Fields are read like the reference reader (lines split at '\n',
+ * fields at white space, reals by atof, integers by atoi): the values are
+ * bit-identical to its.  Printers write "<name>_0.txt" (the reference's
+ * "<name>_<rank>.txt" on a single rank) with "%.15e" reals, byte-identical
+ * to its printers.  The reference reader aborts the process on a malformed
+ * file; these return UNAP_CUDA_EINVAL with its message instead. */
+
+/* constructLDUMatrixFromOpenFOAM (tools/readData/readFromOpenFOAM/
+ * readFromOpenFOAM.cpp:9-139): header "nCells: N nnz: M symm: s", N diagonal
+ * lines "i i diag", then "l u upper [lower]" per face.  *handle receives a
+ * matrix handle like ldumatrixcreat_'s (built on the device on first use);
+ * unap_cuda_matrix_size / unap_cuda_matrix_get_ldu return its arrays. */
+int unap_cuda_read_ldu_matrix(const char* fileName, long int* handle);
+/* constructVectorFromOpenFOAM (readFromOpenFOAM.cpp:142-204): header
+ * "nCells: N", then one value per line; N must equal n. */
+int unap_cuda_read_vector(const char* fileName, long long n, double* v);
+/* constructLDUInterfacesFromOpenFOAM (readFromOpenFOAM.cpp:207-322): header
+ * with nNeiProcs in field 2 and the total face count in field 5, then per
+ * neighbour "processor: <rank> size: <m>" and m lines "faceCell coeff".
+ * Sizes are always returned; each non-NULL array is filled (neighbour and
+ * size hold nNeiProcs entries, faceCells and coeffs nFaces).  Coefficients
+ * are stored negated, as the reference's patches keep them.  Call once with
+ * NULL arrays to size them. */
+int unap_cuda_read_interfaces(const char* fileName, int* nNeiProcs, long long* nFaces,
+                              int* neighbour, int* size, int* faceCells, double* coeffs);
+/* printLDUMatrix (tools/printData/printUNAP/printUNAP.cpp:8-58) */
+int unap_cuda_print_ldu_matrix(long int handle, const char* name);
+/* printVector (printUNAP.hpp:27-42) */
+int unap_cuda_print_vector(const char* name, long long n, const double* v);
+/* printInterfaces (printUNAP.cpp:61-87), from the arrays
+ * unap_cuda_read_interfaces returns.  Its header line carries only
+ * nNeiProcs, so like the reference's, its output is not a file the reader
+ * accepts. */
+int unap_cuda_print_interfaces(const char* name, int nNeiProcs, const int* neighbour,
+                               const int* size, const int* faceCells, const double* coeffs);
+
 #ifdef __cplusplus
 }
 #endif

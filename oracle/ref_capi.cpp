@@ -28,6 +28,8 @@
 #include "lduAgglomeration.hpp"
 #include "eigenDiagPCG.hpp"
 #include "matrixConversion.hpp"
+#include "readFromOpenFOAM.hpp"
+#include "printUNAP.hpp"
 
 using namespace UNAP;
 
@@ -353,5 +355,58 @@ void ref_ldu_get(void* Av, int* l, int* u, double* lower, double* diag, double* 
 }
 
 void ref_ldu_destroy(void* Av) { delete (lduMatrix*)Av; }
+
+/* ---- text dumps: the reference reader and printers, unchanged ---- */
+
+void* ref_read_ldu(const char* path)
+{
+    lduMatrix* A = new lduMatrix;
+    constructLDUMatrixFromOpenFOAM(*A, path);
+    return A;
+}
+
+int ref_ldu_ncells(void* Av) { return (int)((lduMatrix*)Av)->size(); }
+int ref_ldu_symm(void* Av) { return ((lduMatrix*)Av)->symm() ? 1 : 0; }
+
+void ref_read_vector(const char* path, int n, double* out)
+{
+    scalarField b(n);
+    constructVectorFromOpenFOAM(b, path);
+    for (int i = 0; i < n; ++i) out[i] = b[i];
+}
+
+void ref_print_ldu(void* Av, const char* name) { printLDUMatrix(*(lduMatrix*)Av, name); }
+
+void ref_print_vector(const char* name, int n, const double* v)
+{
+    scalarField b(n);
+    for (int i = 0; i < n; ++i) b[i] = v[i];
+    printVector(b, name);
+}
+
+/* reads an interfaces file into a matrix (sizes via the first call with
+ * NULL arrays), copies its patches out and prints them back with
+ * printInterfaces when name != NULL */
+int ref_read_interfaces(const char* path, int* nNei, int* nFaces, int* neighbour, int* size,
+                        int* faceCells, double* coeffs, const char* name)
+{
+    lduMatrix A;
+    constructLDUInterfacesFromOpenFOAM(A, path);
+    const interfaces& I = A.matrixInterfaces();
+    int np = (int)I.size(), k = 0;
+    for (int i = 0; i < np; ++i) {
+        patch& P = I.patchList(i);
+        if (neighbour) neighbour[i] = (int)P.neighbProcNo();
+        if (size) size[i] = (int)P.size();
+        for (label f = 0; f < P.size(); ++f, ++k) {
+            if (faceCells) faceCells[k] = (int)P.faceCells()[f];
+            if (coeffs) coeffs[k] = P.patchCoeffs(f);
+        }
+    }
+    *nNei = np;
+    *nFaces = k;
+    if (name) printInterfaces(A, name);
+    return 0;
+}
 
 }  // extern "C"

@@ -122,6 +122,13 @@ SIGNATURES = {
                                          _c_int, _c_dbl, _c_int, ctypes.POINTER(_c_ll)]),
     "unap_cuda_server_wait": (_c_int, [_c_long, _c_ll, _vp, _vp]),
     "unap_cuda_server_destroy": (_c_int, [_c_long]),
+    "unap_cuda_read_ldu_matrix": (_c_int, [ctypes.c_char_p, _lp]),
+    "unap_cuda_read_vector": (_c_int, [ctypes.c_char_p, _c_ll, _vp]),
+    "unap_cuda_read_interfaces": (_c_int, [ctypes.c_char_p, _ip, ctypes.POINTER(_c_ll), _vp, _vp,
+                                           _vp, _vp]),
+    "unap_cuda_print_ldu_matrix": (_c_int, [_c_long, ctypes.c_char_p]),
+    "unap_cuda_print_vector": (_c_int, [ctypes.c_char_p, _c_ll, _vp]),
+    "unap_cuda_print_interfaces": (_c_int, [ctypes.c_char_p, _c_int, _vp, _vp, _vp, _vp]),
 }
 
 
@@ -586,3 +593,69 @@ def coo2ldumatrixcreat(data, rows_1based, cols_1based, n_cells, symm) -> int:
 
 def sw_matrix_destroy(handle: int) -> None:
     load().sw_matrix_destroy__(ctypes.byref(_c_long(handle)))
+
+
+# ---- text dumps in the reference's on-disk formats (host only)
+
+def _path(p) -> bytes:
+    return os.fsencode(p)
+
+
+def read_ldu_matrix(file_name) -> int:
+    """constructLDUMatrixFromOpenFOAM (readFromOpenFOAM.cpp:9-139): a matrix
+    handle read from an LDU text dump (destroy with sw_matrix_destroy)."""
+    lib = load()
+    h = _c_long(0)
+    check(lib.unap_cuda_read_ldu_matrix(_path(file_name), ctypes.byref(h)))
+    return h.value
+
+
+def read_vector(file_name, n: int) -> np.ndarray:
+    """constructVectorFromOpenFOAM (readFromOpenFOAM.cpp:142-204) into a new
+    array of n values; the file's count must equal n."""
+    v = np.zeros(n)
+    check(load().unap_cuda_read_vector(_path(file_name), n, v.ctypes.data))
+    return v
+
+
+def read_interfaces(file_name) -> dict:
+    """constructLDUInterfacesFromOpenFOAM (readFromOpenFOAM.cpp:207-322):
+    per-neighbour ranks and sizes, then every face's cell and (negated)
+    coefficient."""
+    lib = load()
+    np_ = _c_int()
+    nf = _c_ll()
+    check(lib.unap_cuda_read_interfaces(_path(file_name), ctypes.byref(np_), ctypes.byref(nf),
+                                        None, None, None, None))
+    nb = np.zeros(np_.value, np.int32)
+    sz = np.zeros(np_.value, np.int32)
+    fc = np.zeros(nf.value, np.int32)
+    co = np.zeros(nf.value)
+    check(lib.unap_cuda_read_interfaces(_path(file_name), ctypes.byref(np_), ctypes.byref(nf),
+                                        nb.ctypes.data, sz.ctypes.data, fc.ctypes.data,
+                                        co.ctypes.data))
+    return dict(neighbour=nb, size=sz, face_cells=fc, coeffs=co)
+
+
+def print_ldu_matrix(handle: int, name) -> str:
+    """printLDUMatrix (printUNAP.cpp:8-58); returns the file written."""
+    check(load().unap_cuda_print_ldu_matrix(handle, _path(name)))
+    return os.fsdecode(_path(name)) + "_0.txt"
+
+
+def print_vector(v, name) -> str:
+    """printVector (printUNAP.hpp:27-42); returns the file written."""
+    a = _f64(v)
+    check(load().unap_cuda_print_vector(_path(name), a.shape[0], a.ctypes.data))
+    return os.fsdecode(_path(name)) + "_0.txt"
+
+
+def print_interfaces(name, neighbour, size, face_cells, coeffs) -> str:
+    """printInterfaces (printUNAP.cpp:61-87); returns the file written."""
+    nb, sz, fc = _i32(neighbour), _i32(size), _i32(face_cells)
+    co = _f64(coeffs)
+    if int(sz.sum()) != fc.shape[0] or fc.shape[0] != co.shape[0] or nb.shape != sz.shape:
+        raise ValueError("interface arrays disagree in size")
+    check(load().unap_cuda_print_interfaces(_path(name), nb.shape[0], nb.ctypes.data,
+                                            sz.ctypes.data, fc.ctypes.data, co.ctypes.data))
+    return os.fsdecode(_path(name)) + "_0.txt"
