@@ -168,6 +168,18 @@ int unap_cuda_matrix_get_ldu(long int handle, int* lowerAddr, int* upperAddr, do
 int unap_cuda_matrix_info(long int handle, int* nWavefronts, long long* nEntries,
                           long long* deviceBytes);
 
+/* Internal cell order of a matrix: *nWavefronts forward wavefronts;
+ * perm[i] (nCells entries) is the cell stored at internal row i and
+ * waveStart (nWavefronts + 1 entries) the wavefront boundaries.  Builds the
+ * matrix on the device if it is not built yet.  No reference counterpart. */
+int unap_cuda_matrix_layout(long int handle, int* nWavefronts, int* perm, int* waveStart);
+/* Matrices (and AMG levels) of at least minCells cells build their device
+ * structure (internal order, SELL-32 layout, values) with kernels instead
+ * of host loops; minCells < 0 builds every one on the host.  Both give the
+ * same structure bit for bit.  Default 32768; the previous value is
+ * returned through the (nullable) pointer.  No reference counterpart. */
+int unap_cuda_set_device_setup(long long minCells, long long* oldMinCells);
+
 /* Kernels on device vectors in the caller's cell order (FP64). */
 int unap_cuda_spmv(long int handle, const double* x, double* y);
 /* y = A x like unap_cuda_spmv, for callers that cannot allocate device memory
@@ -222,6 +234,10 @@ void unap_cuda_amg_default_params(unap_cuda_amg_params* p);
 /* builds the hierarchy of an existing matrix handle (the matrix must outlive
  * the AMG handle) */
 int unap_cuda_amg_create(long int* amg, long int matrix, const unap_cuda_amg_params* p);
+/* Internal cell order of AMG level `level` (0 = the matrix), as
+ * unap_cuda_matrix_layout gives it. */
+int unap_cuda_amg_level_layout(long int amg, int level, int* nCells, int* nWavefronts, int* perm,
+                               int* waveStart);
 /* nLevels including the finest; cells[k] for k < min(nLevels, maxOut) */
 int unap_cuda_amg_info(long int amg, int* nLevels, int* cells, int* wavefronts, int maxOut,
                        double* setupSeconds, long long* deviceBytes);

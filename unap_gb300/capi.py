@@ -122,6 +122,9 @@ SIGNATURES = {
                                          _c_int, _c_dbl, _c_int, ctypes.POINTER(_c_ll)]),
     "unap_cuda_server_wait": (_c_int, [_c_long, _c_ll, _vp, _vp]),
     "unap_cuda_server_destroy": (_c_int, [_c_long]),
+    "unap_cuda_set_device_setup": (_c_int, [_c_ll, ctypes.POINTER(_c_ll)]),
+    "unap_cuda_matrix_layout": (_c_int, [_c_long, _ip, _vp, _vp]),
+    "unap_cuda_amg_level_layout": (_c_int, [_c_long, _c_int, _ip, _ip, _vp, _vp]),
     "unap_cuda_read_ldu_matrix": (_c_int, [ctypes.c_char_p, _lp]),
     "unap_cuda_read_vector": (_c_int, [ctypes.c_char_p, _c_ll, _vp]),
     "unap_cuda_read_interfaces": (_c_int, [ctypes.c_char_p, _ip, ctypes.POINTER(_c_ll), _vp, _vp,
@@ -317,6 +320,37 @@ def get_tail_rows(precision: int) -> tuple[int, int]:
     return old[precision]
 
 
+def set_device_setup(min_cells: int) -> int:
+    """Matrices and AMG levels of at least min_cells cells build their device
+    structure with kernels (< 0: all on the host); returns the old value."""
+    old = _c_ll()
+    check(load().unap_cuda_set_device_setup(int(min_cells), ctypes.byref(old)))
+    return old.value
+
+
+def _layout(fn, *head):
+    nw = _c_int()
+    n = _c_int()
+    if fn == "unap_cuda_matrix_layout":
+        lib = load()
+        check(lib.unap_cuda_matrix_layout(*head, ctypes.byref(nw), None, None))
+        info = _c_int()
+        size = _c_int()
+        check(lib.unap_cuda_matrix_size(*head, ctypes.byref(size), ctypes.byref(info), None))
+        perm = np.zeros(size.value, np.int32)
+        ws = np.zeros(nw.value + 1, np.int32)
+        check(lib.unap_cuda_matrix_layout(*head, ctypes.byref(nw), perm.ctypes.data,
+                                          ws.ctypes.data))
+        return perm, ws
+    lib = load()
+    check(lib.unap_cuda_amg_level_layout(*head, ctypes.byref(n), ctypes.byref(nw), None, None))
+    perm = np.zeros(n.value, np.int32)
+    ws = np.zeros(nw.value + 1, np.int32)
+    check(lib.unap_cuda_amg_level_layout(*head, ctypes.byref(n), ctypes.byref(nw),
+                                         perm.ctypes.data, ws.ctypes.data))
+    return perm, ws
+
+
 def tail_cluster_size() -> int:
     """CTAs per cluster of the tail kernel on the current device (0: none)."""
     c = _c_int()
@@ -359,6 +393,10 @@ class DeviceAmg:
                                         waves.ctypes.data, 64, ctypes.byref(t), ctypes.byref(b)))
         return dict(n_levels=n.value, cells=cells[:n.value].tolist(),
                     wavefronts=waves[:n.value].tolist(), setup_s=t.value, device_bytes=b.value)
+
+    def level_layout(self, level: int):
+        """(perm, waveStart) of AMG level `level` (0 = the matrix)."""
+        return _layout("unap_cuda_amg_level_layout", self.handle, level)
 
     def vcycle(self, r, z):
         check(load().unap_cuda_amg_vcycle(self.handle, _ptr(r), _ptr(z)))
@@ -472,6 +510,10 @@ class DeviceMatrix:
         check(load().unap_cuda_matrix_info(self.handle, ctypes.byref(w), ctypes.byref(e),
                                            ctypes.byref(b)))
         return dict(n_wavefronts=w.value, n_entries=e.value, device_bytes=b.value)
+
+    def layout(self):
+        """(perm, waveStart): internal row i holds cell perm[i]."""
+        return _layout("unap_cuda_matrix_layout", self.handle)
 
     def spmv(self, x, y):
         check(load().unap_cuda_spmv(self.handle, _ptr(x), _ptr(y)))

@@ -116,7 +116,10 @@ void put_stats(const SolveStats& s, unap_cuda_stats* o)
 // (matrixConversion.cpp:38-98): 0-based, row-grouped COO of a structurally
 // symmetric matrix -> owner-sorted LDU.  Upper faces come from the (row < col)
 // entries in row-major order; the lower coefficient of face (c, r) is the
-// (r, c) entry, grouped by owner c in order of appearance.
+// (r, c) entry, grouped by owner c in order of appearance.  Input the
+// reference leaves undefined is an error: rows out of order, a repeated
+// entry, a column whose lower entries do not number its upper faces.  The
+// device form (coo_dev.cu) gives the same arrays.
 HostLdu coo_to_ldu(const double* val, const std::vector<int>& row0, const std::vector<int>& col0,
                    int n, int size, bool symm)
 {
@@ -127,6 +130,9 @@ HostLdu coo_to_ldu(const double* val, const std::vector<int>& row0, const std::v
             throw std::invalid_argument("COO entry out of range");
         cnt[(size_t)row0[(size_t)i] + 1]++;
     }
+    for (int i = 1; i < size; ++i)
+        if (row0[(size_t)i - 1] > row0[(size_t)i])
+            throw std::invalid_argument("COO entries must be grouped by row in ascending row order");
     for (int c = 0; c < n; ++c) cnt[(size_t)c + 1] += cnt[(size_t)c];
     std::vector<int> rows((size_t)size), cols((size_t)size);
     std::vector<double> vals((size_t)size);
@@ -134,8 +140,10 @@ HostLdu coo_to_ldu(const double* val, const std::vector<int>& row0, const std::v
         int r = row0[(size_t)i];
         int start = cnt[(size_t)r], len = cnt[(size_t)r + 1] - cnt[(size_t)r];
         int pos = 0;
-        for (int k = 0; k < len; ++k)
-            if (col0[(size_t)i] > col0[(size_t)(start + k)]) pos++;
+        for (int k = 0; k < len; ++k) {
+            int ck = col0[(size_t)(start + k)];
+            if (col0[(size_t)i] > ck || (start + k < i && col0[(size_t)i] == ck)) pos++;
+        }
         rows[(size_t)(start + pos)] = r;
         cols[(size_t)(start + pos)] = col0[(size_t)i];
         vals[(size_t)(start + pos)] = val[i];
@@ -152,6 +160,8 @@ HostLdu coo_to_ldu(const double* val, const std::vector<int>& row0, const std::v
     std::vector<int> upperNbrs((size_t)n, 0);
     for (int i = 0; i < size; ++i) {
         int r = rows[(size_t)i], c = cols[(size_t)i];
+        if (i && rows[(size_t)i - 1] == r && cols[(size_t)i - 1] >= c)
+            throw std::invalid_argument("COO matrix repeats an entry");
         if (r == c) {
             h.diag[(size_t)r] = vals[(size_t)i];
         } else if (c > r) {
@@ -173,6 +183,11 @@ HostLdu coo_to_ldu(const double* val, const std::vector<int>& row0, const std::v
             throw std::invalid_argument("COO matrix is not structurally symmetric");
         std::vector<int> off((size_t)n + 1, 0), c2((size_t)n, 0);
         for (int c = 0; c < n; ++c) off[(size_t)c + 1] = off[(size_t)c] + upperNbrs[(size_t)c];
+        for (int o : lowerCol) c2[(size_t)o]++;
+        for (int c = 0; c < n; ++c)
+            if (c2[(size_t)c] != upperNbrs[(size_t)c])
+                throw std::invalid_argument("COO matrix is not structurally symmetric");
+        std::fill(c2.begin(), c2.end(), 0);
         h.lower.assign((size_t)h.nf, 0.0);
         for (size_t k = 0; k < lowerVal.size(); ++k) {
             int o = lowerCol[k];
@@ -216,15 +231,20 @@ void coo2ldumatrixcreat_(long int* APtrPtr, const double* dataPtr, const int* ro
                          const int* columnPtr, const int* nCells, const int* size, const int* symm)
 {
     int rc = guarded([&] {
-        std::vector<int> r((size_t)*size), c((size_t)*size);
-        for (int i = 0; i < *size; ++i) {
-            r[(size_t)i] = rowsPtr[i] - 1;  // fortranInterface.cpp:90-95
-            c[(size_t)i] = columnPtr[i] - 1;
+        auto m = std::make_unique<MatHandle>();
+        const long long minCells = device_setup_min_cells();
+        if (!(minCells >= 0 && *nCells >= minCells &&
+              coo_to_ldu_device(dataPtr, rowsPtr, columnPtr, *nCells, *size, *symm != 0, false,
+                                0, m->pending))) {
+            std::vector<int> r((size_t)*size), c((size_t)*size);
+            for (int i = 0; i < *size; ++i) {
+                r[(size_t)i] = rowsPtr[i] - 1;  // fortranInterface.cpp:90-95
+                c[(size_t)i] = columnPtr[i] - 1;
+            }
+            m->pending = coo_to_ldu(dataPtr, r, c, *nCells, *size, *symm != 0);
         }
-        auto* m = new MatHandle;
-        m->pending = coo_to_ldu(dataPtr, r, c, *nCells, *size, *symm != 0);
         m->hasValues = true;
-        *APtrPtr = reinterpret_cast<long int>(m);
+        *APtrPtr = reinterpret_cast<long int>(m.release());
     });
     if (rc) {
         std::fprintf(stderr, "unap_cuda: coo2ldumatrixcreat_ failed: %s\n", last_error());
@@ -238,13 +258,23 @@ void csr2ldumatrixcreat_(long int* APtrPtr, const double* dataPtr, const int* co
     int rc = guarded([&] {
         // csr2ldu (coo2ldu.cpp:116-148) expands the row pointer and calls
         // coo2ldu without re-sorting; indices are used as given (0-based)
-        std::vector<int> r((size_t)*size), c(columnPtr, columnPtr + *size);
-        for (int i = 0; i < *nCells; ++i)
-            for (int j = compRowsPtr[i]; j < compRowsPtr[i + 1]; ++j) r[(size_t)j] = i;
-        auto* m = new MatHandle;
-        m->pending = coo_to_ldu(dataPtr, r, c, *nCells, *size, *symm != 0);
+        auto m = std::make_unique<MatHandle>();
+        const long long minCells = device_setup_min_cells();
+        if (!(minCells >= 0 && *nCells >= minCells &&
+              coo_to_ldu_device(dataPtr, compRowsPtr, columnPtr, *nCells, *size, *symm != 0, true,
+                                0, m->pending))) {
+            if (compRowsPtr[0] != 0 || compRowsPtr[*nCells] != *size)
+                throw std::invalid_argument("CSR row pointer is not a valid partition of the entries");
+            std::vector<int> r((size_t)*size), c(columnPtr, columnPtr + *size);
+            for (int i = 0; i < *nCells; ++i) {
+                if (compRowsPtr[i + 1] < compRowsPtr[i])
+                    throw std::invalid_argument("CSR row pointer is not a valid partition of the entries");
+                for (int j = compRowsPtr[i]; j < compRowsPtr[i + 1]; ++j) r[(size_t)j] = i;
+            }
+            m->pending = coo_to_ldu(dataPtr, r, c, *nCells, *size, *symm != 0);
+        }
         m->hasValues = true;
-        *APtrPtr = reinterpret_cast<long int>(m);
+        *APtrPtr = reinterpret_cast<long int>(m.release());
     });
     if (rc) {
         std::fprintf(stderr, "unap_cuda: csr2ldumatrixcreat_ failed: %s\n", last_error());
@@ -484,6 +514,24 @@ int unap_cuda_matrix_get_ldu(long int handle, int* lowerAddr, int* upperAddr, do
         if (upper) std::memcpy(upper, H.upper.data(), nf * sizeof(double));
         if (lower) std::memcpy(lower, H.lowerPtr(), nf * sizeof(double));
         if (diag) std::memcpy(diag, H.diag.data(), n * sizeof(double));
+    });
+}
+
+int unap_cuda_set_device_setup(long long minCells, long long* oldMinCells)
+{
+    return guarded([&] {
+        long long o = set_device_setup_min_cells(minCells);
+        if (oldMinCells) *oldMinCells = o;
+    });
+}
+
+int unap_cuda_matrix_layout(long int handle, int* nWavefronts, int* perm, int* waveStart)
+{
+    return guarded([&] {
+        const Level& L = *mat_from(handle)->get().L;
+        if (nWavefronts) *nWavefronts = L.nWave;
+        if (perm) std::memcpy(perm, L.perm.data(), sizeof(int) * L.perm.size());
+        if (waveStart) std::memcpy(waveStart, L.waveStart.data(), sizeof(int) * L.waveStart.size());
     });
 }
 

@@ -84,6 +84,14 @@ std::vector<int> bfs_rank(int n, const std::vector<int>& loStart, const std::vec
 std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key,
                                    bool identityOrder, cudaStream_t s)
 {
+    const long long minCells = device_setup_min_cells();
+    if (!identityOrder && A.oriented && A.ownerSorted && minCells >= 0 && A.n > 0 &&
+        A.n >= minCells) {
+        if (auto D = build_level_device(A, key, s)) {
+            D->version = next_version();
+            return D;
+        }
+    }
     auto L = std::make_unique<Level>();
     L->version = next_version();
     const int n = A.n, nf = A.nf;

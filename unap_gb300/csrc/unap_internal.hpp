@@ -143,6 +143,20 @@ void update_level_values(Level& L, const HostLdu& A, cudaStream_t s);
 std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key,
                                    bool identityOrder, cudaStream_t s);
 void make_fp32(Level& L, cudaStream_t s);
+// The same Level built by kernels on stream s (level_dev.cu); nullptr when
+// the matrix has a shape the device build leaves to the host.
+std::unique_ptr<Level> build_level_device(const HostLdu& A, const std::vector<int>* key,
+                                          cudaStream_t s);
+// Levels of at least this many cells are built on the device (< 0: none).
+long long set_device_setup_min_cells(long long minCells);
+long long device_setup_min_cells();
+// out[i] = in[0] + ... + in[i-1] for i <= n (n + 1 outputs), on stream s
+void device_exclusive_scan(const int* in, int* out, long long n, cudaStream_t s);
+// COO (1-based rows and columns) or CSR (0-based row pointer and columns)
+// to LDU on the device, bit-identical to the host form; false when it
+// declines (a column with too many lower entries) and nothing was done.
+bool coo_to_ldu_device(const double* val, const int* rowsOrPtr, const int* cols, int n, int size,
+                       bool symm, bool csr, cudaStream_t s, HostLdu& out);
 
 // Solver state shared by the device kernels of one solve (device memory).
 // Every kernel of an iteration first checks `done` (and `early` where the
