@@ -13,12 +13,37 @@
 #include <cmath>
 #include <cstring>
 #include <stdexcept>
+#include <thread>
 
 #include "amg.hpp"
 
 namespace unapgpu {
 
 static constexpr double kSmall = 1.0e-37;  // SMALL, src/base/unap.hpp:88
+
+namespace {
+
+// f(begin, end) over [0, n) split across host threads (at least minPer
+// items each)
+template <class F>
+void parallel_ranges(int n, int minPer, F&& f)
+{
+    unsigned hw = std::thread::hardware_concurrency();
+    int nt = (int)std::min<long long>({(long long)(hw ? hw : 1), 32LL, (long long)n / minPer});
+    if (nt <= 1) {
+        f(0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve((size_t)nt);
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back([&, t] {
+            f((int)((long long)n * t / nt), (int)((long long)n * (t + 1) / nt));
+        });
+    for (auto& x : th) x.join();
+}
+
+}  // namespace
 
 std::vector<int> pairwise_pass(const HostLdu& A, const std::vector<double>& w, int& nCoarse)
 {
@@ -76,70 +101,76 @@ std::vector<int> pairwise_pass(const HostLdu& A, const std::vector<double>& w, i
     return map;
 }
 
+// Coarse faces are numbered by coarse owner, then by the order in which
+// each owner's fine boundary faces (in fine face order) first meet a
+// neighbour -- the reference's numbering.  Owners are independent, so after
+// two serial counting passes the owners are split over host threads.
 void coarse_addressing(const HostLdu& fine, const std::vector<int>& map, int nCoarse,
                        CoarseHost& out)
 {
     const int nf = fine.nf;
     const int* l = fine.l.data();
     const int* u = fine.u.data();
+    const int* mp = map.data();
     out.faceRestrict.assign((size_t)nf, 0);
-    // segment of every coarse owner, sized by its fine boundary faces
+    // coarse owner of every fine boundary face (-1: inside an aggregate)
+    std::vector<int> own((size_t)nf);
+    parallel_ranges(nf, 65536, [&](int f0, int f1) {
+        for (int f = f0; f < f1; ++f) {
+            int a = mp[u[f]], b = mp[l[f]];
+            own[(size_t)f] = a != b ? std::min(a, b) : -1;
+            if (a == b) out.faceRestrict[(size_t)f] = -(a + 1);
+        }
+    });
+    // fine boundary faces of every coarse owner, in fine face order
     std::vector<int> segStart((size_t)nCoarse + 1, 0);
-    for (int f = 0; f < nf; ++f) {
-        int a = map[(size_t)u[f]], b = map[(size_t)l[f]];
-        if (a != b) segStart[(size_t)std::min(a, b) + 1]++;
-    }
+    for (int f = 0; f < nf; ++f)
+        if (own[(size_t)f] >= 0) segStart[(size_t)own[(size_t)f] + 1]++;
     for (int c = 0; c < nCoarse; ++c) segStart[(size_t)c + 1] += segStart[(size_t)c];
-    std::vector<int> segFace((size_t)segStart[(size_t)nCoarse]);  // provisional coarse face ids
-    std::vector<int> segLen((size_t)nCoarse, 0);
-    std::vector<int> nei;  // neighbour of each provisional coarse face
-    nei.reserve((size_t)segStart[(size_t)nCoarse]);
-    int nCF = 0;
-    for (int f = 0; f < nf; ++f) {
-        int rmU = map[(size_t)u[f]], rmL = map[(size_t)l[f]];
-        if (rmU == rmL) {
-            out.faceRestrict[(size_t)f] = -(rmU + 1);
-            continue;
-        }
-        int own = rmU, ne = rmL;
-        if (rmU > rmL) {
-            own = rmL;
-            ne = rmU;
-        }
-        int* seg = &segFace[(size_t)segStart[(size_t)own]];
-        int len = segLen[(size_t)own];
-        int found = -1;
-        for (int i = 0; i < len; ++i)
-            if (nei[(size_t)seg[i]] == ne) {
-                found = seg[i];
-                break;
-            }
-        if (found < 0) {
-            found = nCF++;
-            nei.push_back(ne);
-            seg[len] = found;
-            segLen[(size_t)own] = len + 1;
-        }
-        out.faceRestrict[(size_t)f] = found;
+    const size_t total = (size_t)segStart[(size_t)nCoarse];
+    std::vector<int> segFace(total);
+    {
+        std::vector<int> pos(segStart.begin(), segStart.end() - 1);
+        for (int f = 0; f < nf; ++f)
+            if (own[(size_t)f] >= 0) segFace[(size_t)pos[(size_t)own[(size_t)f]]++] = f;
     }
-    // renumber: coarse owners ascending, discovery order inside an owner
-    std::vector<int> renum((size_t)nCF);
+    // per owner: distinct neighbours in discovery order, each boundary
+    // face's index among them
+    std::vector<int> nei(total), local(total), cnt((size_t)nCoarse, 0);
+    parallel_ranges(nCoarse, 4096, [&](int c0, int c1) {
+        for (int c = c0; c < c1; ++c) {
+            const size_t a = (size_t)segStart[(size_t)c], e = (size_t)segStart[(size_t)c + 1];
+            int m = 0;
+            for (size_t i = a; i < e; ++i) {
+                const int f = segFace[i];
+                const int ne = std::max(mp[u[f]], mp[l[f]]);
+                int j = 0;
+                while (j < m && nei[a + (size_t)j] != ne) ++j;
+                if (j == m) nei[a + (size_t)m++] = ne;
+                local[i] = j;
+            }
+            cnt[(size_t)c] = m;
+        }
+    });
+    std::vector<int> cfStart((size_t)nCoarse + 1, 0);
+    for (int c = 0; c < nCoarse; ++c) cfStart[(size_t)c + 1] = cfStart[(size_t)c] + cnt[(size_t)c];
+    const int nCF = cfStart[(size_t)nCoarse];
     out.A.n = nCoarse;
     out.A.nf = nCF;
     out.A.l.resize((size_t)nCF);
     out.A.u.resize((size_t)nCF);
-    int k = 0;
-    for (int c = 0; c < nCoarse; ++c) {
-        const int* seg = &segFace[(size_t)segStart[(size_t)c]];
-        for (int i = 0; i < segLen[(size_t)c]; ++i) {
-            out.A.l[(size_t)k] = c;
-            out.A.u[(size_t)k] = nei[(size_t)seg[i]];
-            renum[(size_t)seg[i]] = k++;
+    parallel_ranges(nCoarse, 4096, [&](int c0, int c1) {
+        for (int c = c0; c < c1; ++c) {
+            const size_t a = (size_t)segStart[(size_t)c];
+            const int k0 = cfStart[(size_t)c];
+            for (int j = 0; j < cnt[(size_t)c]; ++j) {
+                out.A.l[(size_t)(k0 + j)] = c;
+                out.A.u[(size_t)(k0 + j)] = nei[a + (size_t)j];
+            }
+            for (size_t i = a; i < (size_t)segStart[(size_t)c + 1]; ++i)
+                out.faceRestrict[(size_t)segFace[i]] = k0 + local[i];
         }
-    }
-    for (int f = 0; f < nf; ++f)
-        if (out.faceRestrict[(size_t)f] >= 0)
-            out.faceRestrict[(size_t)f] = renum[(size_t)out.faceRestrict[(size_t)f]];
+    });
     out.restrictAddr = map;
 }
 
