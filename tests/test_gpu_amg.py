@@ -137,3 +137,26 @@ def test_amg_rejects_nonsymmetric(cuda):
     with pytest.raises(capi.UnapCudaError, match="symmetric"):
         capi.DeviceAmg(A)
     A.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_device_coarsest_inverse_bit_exact(cuda, orc, precision):
+    """Coarsest levels of 128 cells or more are inverted on the device; the
+    V-cycle stays bit-identical to the oracle's, with coarse levels and with
+    none (the matrix itself is the coarsest, in its own internal order)."""
+    torch = cuda
+    for s, nco in ((W.lognormal(18, 16, 14, seed=12, permute=True), 700),
+                   (W.laplace(8, 8, 6, seed=13, permute=True, rhs="normal"), 1000)):
+        A = capi.DeviceMatrix(s)
+        G = capi.DeviceAmg(A, n_coarsest=nco, precision=precision)
+        O = OracleAmg(orc, s, n_coarsest=nco, precision=precision)
+        cells = G.info()["cells"]
+        assert cells == O.level_sizes(), s.name
+        assert cells[-1] >= 128, cells
+        r = np.random.default_rng(s.n).standard_normal(s.n)
+        z = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+        G.vcycle(dev(torch, r), z)
+        assert np.array_equal(z.cpu().numpy(), O.vcycle(r)), (s.name, precision)
+        G.close()
+        O.close()
+        A.close()

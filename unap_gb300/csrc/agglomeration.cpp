@@ -216,7 +216,8 @@ void coarse_coefficients(const HostLdu& fine, CoarseHost& c)
 }
 
 std::vector<CoarseHost> agglomerate_levels(const HostLdu& fine, const std::vector<double>& weights,
-                                           int nCoarsest, int maxLevels, int stopRule)
+                                           int nCoarsest, int maxLevels, int stopRule,
+                                           cudaStream_t s)
 {
     if (maxLevels <= 0) maxLevels = 50;
     if (nCoarsest <= 0) nCoarsest = 50;
@@ -225,6 +226,19 @@ std::vector<CoarseHost> agglomerate_levels(const HostLdu& fine, const std::vecto
     while ((int)levels.size() < maxLevels - 1) {
         const HostLdu& fm = levels.empty() ? fine : levels.back().A;
         if (stopRule == 1 && fm.n <= nCoarsest) break;
+        const long long minCells = device_setup_min_cells();
+        if (minCells >= 0 && fm.n >= minCells) {
+            CoarseHost c;
+            std::vector<double> cw;
+            int nc = -1;
+            if (agglomerate_level_device(fm, w, c, cw, nc, s)) {
+                bool keep = stopRule == 1 ? (nc < fm.n) : (nc >= nCoarsest);
+                if (!keep) break;
+                w.swap(cw);
+                levels.push_back(std::move(c));
+                continue;
+            }
+        }
         int nc = -1;
         std::vector<int> map = pairwise_pass(fm, w, nc);
         bool keep = stopRule == 1 ? (nc < fm.n) : (nc >= nCoarsest);

@@ -39,7 +39,7 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
     cudaStream_t s = A.stream;
     std::vector<double> w = mg_face_weights(A.host);
     std::vector<CoarseHost> coarse =
-        agglomerate_levels(A.host, w, params.nCoarsest, params.maxLevels, 1);
+        agglomerate_levels(A.host, w, params.nCoarsest, params.maxLevels, 1, s);
     const int L = (int)coarse.size();
     lv.resize((size_t)L + 1);
     lv[0].L = A.L.get();
@@ -95,16 +95,27 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
             dense[(size_t)Ch.l[(size_t)f] * N + Ch.u[(size_t)f]] += Ch.upper[(size_t)f];
             dense[(size_t)Ch.u[(size_t)f] * N + Ch.l[(size_t)f]] += Ch.lowerPtr()[f];
         }
-        if (!dense_spd_inverse(nc, dense, inv))
-            throw std::invalid_argument("coarsest matrix is not positive definite");
-        // column-major copy in the coarsest level's internal order (identity
-        // when L >= 1; the finest level's order when no coarse level exists)
+        // column-major copy with rows in the coarsest level's internal order
+        // and columns in its own cell order: column j, row I holds
+        // inv[perm[I]][j].  The product then sums each row in cell order,
+        // gathering b through iperm (identity, so no gather, when L >= 1;
+        // the finest level's order when no coarse level exists).
         const Level& CL = *lv[(size_t)L].L;
-        std::vector<double> cm(N * N);
-        for (int J = 0; J < nc; ++J)
-            for (int I = 0; I < nc; ++I)
-                cm[(size_t)J * N + I] = inv[(size_t)CL.perm[(size_t)I] * N + CL.perm[(size_t)J]];
-        Minv.upload(cm, s);
+        denseGather = L ? nullptr : CL.d_iperm.p;
+        if (nc >= kDeviceInverseCells) {
+            // the same bits computed on the device (dense_dev.cu)
+            Minv.alloc(N * N);
+            if (!dense_spd_inverse_device(nc, dense, CL.d_iperm.p, Minv.p, s))
+                throw std::invalid_argument("coarsest matrix is not positive definite");
+        } else {
+            if (!dense_spd_inverse(nc, dense, inv))
+                throw std::invalid_argument("coarsest matrix is not positive definite");
+            std::vector<double> cm(N * N);
+            for (int j = 0; j < nc; ++j)
+                for (int I = 0; I < nc; ++I)
+                    cm[(size_t)j * N + I] = inv[(size_t)CL.perm[(size_t)I] * N + (size_t)j];
+            Minv.upload(cm, s);
+        }
     }
     {
         std::vector<int> all;
@@ -311,7 +322,7 @@ void AmgHierarchy::vcycle_level(const Exec& ex, int k, Gate g)
         return;
     }
     if (k == L) {
-        k_dense_apply<T>(ex, nc, Minv.p, b, x, g);
+        k_dense_apply<T>(ex, nc, Minv.p, b, denseGather, x, g);
         if (profOut) UNAP_CK(cudaEventRecordWithFlags((*profOut)[(size_t)k], ex.s, cudaEventRecordExternal));
         return;
     }
@@ -352,6 +363,7 @@ void AmgHierarchy::append_level(std::vector<Step>& out, int k, int tableBase)
         Step s = step(ST_DENSE, true);
         s.r1 = nc;
         s.e = Minv.p;
+        s.i0 = denseGather;
         s.a = b;
         s.c = x;
         s.bytes = 8.0 * nc * nc + 2.0 * sizeof(T) * nc;

@@ -22,8 +22,13 @@ void coarse_addressing(const HostLdu& fine, const std::vector<int>& map, int nCo
 void coarse_coefficients(const HostLdu& fine, CoarseHost& c);
 // stopRule 0: the reference's rule (keep a level while it has >= nCoarsest
 // cells); stopRule 1: agglomerate until the coarsest has <= nCoarsest cells.
+// Levels of at least device_setup_min_cells() cells are agglomerated by
+// kernels on stream s (aggl_dev.cu), with the same result.
 std::vector<CoarseHost> agglomerate_levels(const HostLdu& fine, const std::vector<double>& weights,
-                                           int nCoarsest, int maxLevels, int stopRule);
+                                           int nCoarsest, int maxLevels, int stopRule,
+                                           cudaStream_t s = 0);
+bool agglomerate_level_device(const HostLdu& A, const std::vector<double>& w, CoarseHost& out,
+                              std::vector<double>& cw, int& nCoarse, cudaStream_t s);
 std::vector<double> mg_face_weights(const HostLdu& A);
 
 struct AmgParams {
@@ -70,6 +75,7 @@ public:
     };
     std::vector<Lv> lv;
     DevArray<double> Minv;  // coarsest dense inverse, column-major
+    const int* denseGather = nullptr;  // b index of each Minv column (null: identity)
     int nc = 0;
     DevArray<int> dWaves;       // wave starts of every level, concatenated
     std::vector<int> waveOff;   // level k's first entry in dWaves (size levels + 1)

@@ -34,20 +34,7 @@ int grid_for(long long n)
 }
 
 template <class T>
-struct Scratch {
-    T* p = nullptr;
-    cudaStream_t s = 0;
-    Scratch(size_t count, cudaStream_t st) : s(st)
-    {
-        if (count) UNAP_CK(cudaMallocAsync((void**)&p, count * sizeof(T), s));
-    }
-    Scratch(const Scratch&) = delete;
-    Scratch& operator=(const Scratch&) = delete;
-    ~Scratch()
-    {
-        if (p) cudaFreeAsync(p, s);
-    }
-};
+using Scratch = StreamScratch<T>;
 
 // error bits
 constexpr int kBadRange = 1, kBadOrder = 2, kBadDup = 4, kBadSym = 8, kBadBucket = 16,

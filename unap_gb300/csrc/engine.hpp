@@ -110,5 +110,12 @@ int set_default_executor(int persistent);
 // Dense FP64 SPD inverse by Cholesky (row-major in, row-major out).
 // Returns false when the matrix is not positive definite.
 bool dense_spd_inverse(int n, const std::vector<double>& A, std::vector<double>& inv);
+// The same inverse computed on the device (dense_dev.cu), written
+// column-major to out (n * n doubles on the device) with rows in the
+// internal order iperm gives (null: identity) and columns in cell order.
+// Used from this many coarsest cells up.
+constexpr int kDeviceInverseCells = 128;
+bool dense_spd_inverse_device(int n, const std::vector<double>& A, const int* iperm, double* out,
+                              cudaStream_t s);
 
 }  // namespace unapgpu

@@ -600,13 +600,15 @@ void k_prolong_add(const Exec& ex, int nFine, const int* cmap, const T* coarse, 
 // Dense coarsest solve: x_i = sum_j Minv[i][j] b_j, j ascending, FP64.
 // b is staged in shared memory as FP64; thread i walks column-major Minv so
 // a warp reads 32 consecutive rows of one column per step.
+// gather (optional) maps column j to its entry of b, so the sum runs in the
+// column order of M even when b is in another order.
 template <class T>
 __global__ void dense_apply_kernel(int n, const double* __restrict__ M, const T* __restrict__ b,
-                                   T* __restrict__ x, Gate g)
+                                   const int* __restrict__ gather, T* __restrict__ x, Gate g)
 {
     if (gate_closed(g)) return;
     extern __shared__ double sb[];
-    for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = (double)b[j];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = (double)b[gather ? gather[j] : j];
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double t = 0.0;
@@ -617,13 +619,14 @@ __global__ void dense_apply_kernel(int n, const double* __restrict__ M, const T*
 }
 
 template <class T>
-void k_dense_apply(const Exec& ex, int n, const double* MinvColMajor, const T* b, T* x, Gate g)
+void k_dense_apply(const Exec& ex, int n, const double* MinvColMajor, const T* b, const int* gather,
+                   T* x, Gate g)
 {
     if (n <= 0) return;
     int threads = 64;
     int blocks = div_up(n, threads);
-    tick(), dense_apply_kernel<T><<<blocks, threads, (size_t)n * sizeof(double), ex.s>>>(n, MinvColMajor,
-                                                                               b, x, g);
+    tick(), dense_apply_kernel<T><<<blocks, threads, (size_t)n * sizeof(double), ex.s>>>(
+        n, MinvColMajor, b, gather, x, g);
 }
 
 template <class T>
@@ -800,7 +803,7 @@ int device_max_blocks()
     template void k_to_reference<T>(const Exec&, int, const int*, const T*, T*);                  \
     template void k_restrict<T>(const Exec&, int, const int*, const int*, const T*, T*, Gate);    \
     template void k_prolong_add<T>(const Exec&, int, const int*, const T*, T*, Gate);             \
-    template void k_dense_apply<T>(const Exec&, int, const double*, const T*, T*, Gate);          \
+    template void k_dense_apply<T>(const Exec&, int, const double*, const T*, const int*, T*, Gate);          \
     template void k_fill<T>(const Exec&, long long, T*, T);                                        \
     template void k_scaling_sums<T>(const Exec&, int, const T*, const T*, T*, const T*, RSpec,    \
                                     Gate);                                                        \

@@ -89,7 +89,8 @@ template <class T>
 void k_prolong_add(const Exec& ex, int nFine, const int* cmap, const T* coarse, T* fine, Gate g);
 // x = Minv b with Minv column-major n x n FP64, each row summed over ascending columns
 template <class T>
-void k_dense_apply(const Exec& ex, int n, const double* MinvColMajor, const T* b, T* x, Gate g);
+void k_dense_apply(const Exec& ex, int n, const double* MinvColMajor, const T* b, const int* gather,
+                   T* x, Gate g);
 
 // elementwise helpers
 template <class T>

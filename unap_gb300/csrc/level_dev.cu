@@ -50,22 +50,8 @@ int grid_for(long long n, int threads = kThreads)
     return (int)std::max(1LL, std::min(b, 1LL << 30));
 }
 
-// stream-ordered scratch, freed on the stream when it goes out of scope
 template <class T>
-struct Scratch {
-    T* p = nullptr;
-    cudaStream_t s = 0;
-    Scratch(size_t count, cudaStream_t st) : s(st)
-    {
-        if (count) UNAP_CK(cudaMallocAsync((void**)&p, count * sizeof(T), s));
-    }
-    Scratch(const Scratch&) = delete;
-    Scratch& operator=(const Scratch&) = delete;
-    ~Scratch()
-    {
-        if (p) cudaFreeAsync(p, s);
-    }
-};
+using Scratch = StreamScratch<T>;
 
 // ------------------------------------------------------------------ scans
 

@@ -145,7 +145,7 @@ __device__ void exec_dense(const Step& s, int first, int stride, bool single)
     const T* b = (const T*)s.a;
     T* x = (T*)s.c;
     const double* M = (const double*)s.e;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = (double)b[j];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = (double)b[s.i0 ? s.i0[j] : j];
     __syncthreads();
     for (int i = first; i < n; i += stride) {
         double t = 0.0;

@@ -237,7 +237,7 @@ MgSolver::MgSolver(Matrix& A_, const std::vector<double>& weights, const MgParam
     ex.maxBlocks = device_max_blocks();
     scale = params.scaleCorr < 0 ? A.host.symm : (params.scaleCorr != 0);
     std::vector<CoarseHost> coarse =
-        agglomerate_levels(A.host, weights, params.nCoarsest, params.maxLevels, 0);
+        agglomerate_levels(A.host, weights, params.nCoarsest, params.maxLevels, 0, s);
     const int nC = (int)coarse.size();
     lv.resize((size_t)nC + 1);
     lv[0].L = A.L.get();

@@ -96,6 +96,25 @@ struct DevArray {
     size_t bytes() const { return n * sizeof(T); }
 };
 
+// Stream-ordered scratch (cudaMallocAsync), freed on its stream when it
+// goes out of scope; for the setup kernels that must not synchronize the
+// device while other streams are solving.
+template <class T>
+struct StreamScratch {
+    T* p = nullptr;
+    cudaStream_t s = 0;
+    StreamScratch(size_t count, cudaStream_t st) : s(st)
+    {
+        if (count) UNAP_CK(cudaMallocAsync((void**)&p, count * sizeof(T), s));
+    }
+    StreamScratch(const StreamScratch&) = delete;
+    StreamScratch& operator=(const StreamScratch&) = delete;
+    ~StreamScratch()
+    {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
 // Host copy of one LDU matrix in the reference's layout.
 struct HostLdu {
     int n = 0, nf = 0;
