@@ -236,3 +236,55 @@ def test_device_coo_ingest_errors_match_host(cuda):
                     capi.coo2ldumatrixcreat(v, rr + 1, cc + 1, s.n, symm=False)
             finally:
                 capi.set_device_setup(old)
+
+
+def test_device_agglomeration_matches_oracle(cuda, orc):
+    """Agglomeration on the device (dependency rounds of the sequential
+    greedy) gives the reference's hierarchy: level sizes and V-cycle bits
+    equal to the oracle's."""
+    from oracle_lib import OracleAmg
+    torch = cuda
+    old = capi.set_device_setup(1)
+    try:
+        for s in (W.lognormal(30, 26, 24, seed=21, permute=True),
+                  W.laplace(28, seed=22, permute=True, rhs="normal"),
+                  W.lognormal(16, 14, 12, seed=23, permute=False)):
+            for precision in (0, 1):
+                A = capi.DeviceMatrix(s)
+                G = capi.DeviceAmg(A, n_coarsest=60, precision=precision)
+                O = OracleAmg(orc, s, n_coarsest=60, precision=precision)
+                assert G.info()["cells"] == O.level_sizes(), s.name
+                r = np.random.default_rng(s.n).standard_normal(s.n)
+                z = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+                G.vcycle(torch.tensor(r, device="cuda"), z)
+                assert np.array_equal(z.cpu().numpy(), O.vcycle(r)), (s.name, precision)
+                G.close()
+                O.close()
+                A.close()
+    finally:
+        capi.set_device_setup(old)
+
+
+def test_device_agglomeration_asymmetric_mg_same_bits(cuda):
+    """The reference MGSolver on a convection-diffusion matrix (asymmetric
+    coarse coefficients): device-built and host-built hierarchies give the
+    same solve bit for bit."""
+    torch = cuda
+    s = W.convdiff(22, 20, 18, seed=24, permute=True, pe=2.0)
+    w = np.abs(s.upper) / np.sqrt(np.sum(s.upper ** 2))
+    out = []
+    for mc in (1, -1):
+        old = capi.set_device_setup(mc)
+        try:
+            A = capi.DeviceMatrix(s)
+            G = capi.DeviceMG(A, weights=w, smoother=1, n_coarsest=12, rel_tol=1e-8, max_iter=60)
+        finally:
+            capi.set_device_setup(old)
+        x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+        st = G.solve(x, torch.tensor(s.b, device="cuda"))
+        out.append((G.levels(), st["nIterations"], x.cpu().numpy()))
+        G.close()
+        A.close()
+    assert out[0][0] == out[1][0]
+    assert out[0][1] == out[1][1]
+    assert np.array_equal(out[0][2], out[1][2])
