@@ -506,20 +506,23 @@ int AmgHierarchy::profile(cudaStream_t s, int reps, double* ms, int maxOut)
     cudaGraphExec_t ge = nullptr;
     profIn = &in;
     profOut = &out;
-    UNAP_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    set_capturing(true);
-    try {
-        vcycle(ex, r.p, z.p, Gate{});
-    } catch (...) {
+    {
+        CaptureGate gate;
+        UNAP_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        set_capturing(true);
+        try {
+            vcycle(ex, r.p, z.p, Gate{});
+        } catch (...) {
+            set_capturing(false);
+            profIn = profOut = nullptr;
+            cudaStreamEndCapture(s, &gr);
+            if (gr) cudaGraphDestroy(gr);
+            throw;
+        }
         set_capturing(false);
         profIn = profOut = nullptr;
-        cudaStreamEndCapture(s, &gr);
-        if (gr) cudaGraphDestroy(gr);
-        throw;
+        UNAP_CK(cudaStreamEndCapture(s, &gr));
     }
-    set_capturing(false);
-    profIn = profOut = nullptr;
-    UNAP_CK(cudaStreamEndCapture(s, &gr));
     UNAP_CK(cudaGraphInstantiate(&ge, gr, 0));
     UNAP_CK(cudaGraphLaunch(ge, s));
     UNAP_CK(cudaEventRecord(e0, s));

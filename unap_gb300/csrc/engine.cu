@@ -14,6 +14,16 @@ namespace unapgpu {
 
 // ---- error text ---------------------------------------------------------
 static thread_local std::string g_last_error;
+std::shared_mutex& capture_gate()
+{
+    static std::shared_mutex m;
+    return m;
+}
+bool& thread_in_capture()
+{
+    static thread_local bool v = false;
+    return v;
+}
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 const char* last_error() { return g_last_error.c_str(); }
 
@@ -220,8 +230,8 @@ Krylov::Krylov(Matrix& A_, Precond* P_, Method m) : A(A_), P(P_), method(m)
         s.alloc(N);
         t.alloc(N);
     }
-    UNAP_CK(cudaMalloc((void**)&d_st, sizeof(KState)));
-    UNAP_CK(cudaMallocHost((void**)&h_st, sizeof(KState)));
+    UNAP_CK(gated_malloc((void**)&d_st, sizeof(KState)));
+    UNAP_CK(gated_malloc_host((void**)&h_st, sizeof(KState)));
     // partial buffers for one CTA per 256 rows (row kernels launch that many)
     pool.init(S_NSITES, std::max(ex.maxBlocks, div_up(n, kBlock)), std::max(1, A.L->nWave) + 1,
               ex.s);
@@ -233,8 +243,8 @@ Krylov::~Krylov()
 {
     if (graphExec) cudaGraphExecDestroy(graphExec);
     if (graph) cudaGraphDestroy(graph);
-    if (d_st) cudaFree(d_st);
-    if (h_st) cudaFreeHost(h_st);
+    if (d_st) gated_free(d_st);
+    if (h_st) gated_free_host(h_st);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
 }
@@ -404,6 +414,7 @@ void Krylov::enqueueIteration()
 void Krylov::runIterations()
 {
     if (useGraph && !graphExec) {
+        CaptureGate gate;
         UNAP_CK(cudaStreamBeginCapture(ex.s, cudaStreamCaptureModeThreadLocal));
         set_capturing(true);
         try {

@@ -515,12 +515,12 @@ void to_host(std::vector<T>& h, const T* d, size_t n, cudaStream_t s)
     if (n) UNAP_CK(cudaMemcpyAsync(h.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost, s));
 }
 
-// a few device ints read back through one pinned buffer
+// a few device ints read back (pageable: no pinned allocation, which would
+// synchronize the device)
 struct Readback {
-    int* h = nullptr;
+    int h[16] = {};
     cudaStream_t s;
-    explicit Readback(cudaStream_t st) : s(st) { UNAP_CK(cudaMallocHost((void**)&h, 16 * sizeof(int))); }
-    ~Readback() { cudaFreeHost(h); }
+    explicit Readback(cudaStream_t st) : s(st) {}
     int get(const int* d, int slot = 0)
     {
         UNAP_CK(cudaMemcpyAsync(h + slot, d, sizeof(int), cudaMemcpyDeviceToHost, s));

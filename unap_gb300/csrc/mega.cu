@@ -407,13 +407,13 @@ bool mega_single_level(int nRows) { return nRows <= 48 * 1024; }
 
 MegaRunner::MegaRunner()
 {
-    UNAP_CK(cudaMallocHost((void**)&h_status, sizeof(MegaStatus)));
+    UNAP_CK(gated_malloc_host((void**)&h_status, sizeof(MegaStatus)));
     d_status.alloc(1);
 }
 
 MegaRunner::~MegaRunner()
 {
-    if (h_status) cudaFreeHost(h_status);
+    if (h_status) gated_free_host(h_status);
 }
 
 int MegaRunner::threads() const { return kMegaThreads; }

@@ -330,8 +330,8 @@ MgSolver::MgSolver(Matrix& A_, const std::vector<double>& weights, const MgParam
     sfs.alloc((size_t)2 * (nC + 2));
     eig.alloc((size_t)nC + 1);
     chebyFirst.assign((size_t)nC + 1, 1);
-    UNAP_CK(cudaMalloc((void**)&d_st, sizeof(KState)));
-    UNAP_CK(cudaMallocHost((void**)&h_st, sizeof(KState)));
+    UNAP_CK(gated_malloc((void**)&d_st, sizeof(KState)));
+    UNAP_CK(gated_malloc_host((void**)&h_st, sizeof(KState)));
     pool.init(M_NSITES, ex.maxBlocks, 2, s);
     UNAP_CK(cudaEventCreate(&ev0));
     UNAP_CK(cudaEventCreate(&ev1));
@@ -340,8 +340,8 @@ MgSolver::MgSolver(Matrix& A_, const std::vector<double>& weights, const MgParam
 
 MgSolver::~MgSolver()
 {
-    if (d_st) cudaFree(d_st);
-    if (h_st) cudaFreeHost(h_st);
+    if (d_st) gated_free(d_st);
+    if (h_st) gated_free_host(h_st);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
 }

@@ -162,8 +162,9 @@ void Server::largeWorker()
             K.flexible = flexible;
             K.trueResidualRestart = restart;
             // concurrent slots share the SMs: the persistent cooperative
-            // executor needs every SM, so slots launch their steps directly
-            // (no graph capture, which another slot's setup could invalidate)
+            // executor needs every SM, so slots launch their steps directly.
+            // (Graph replay was measured slower here: each capture holds
+            // the capture gate against the other slots' setup allocations.)
             K.useMega = params.maxSlots == 1;
             K.useGraph = false;
             r->tSetup = now_seconds();

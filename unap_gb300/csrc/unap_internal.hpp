@@ -29,6 +29,8 @@
 #include <cstdint>
 #include <cstdio>
 #include <memory>
+#include <mutex>
+#include <shared_mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -49,6 +51,47 @@ struct CudaError : std::runtime_error {
 
 void set_last_error(const std::string& msg);
 const char* last_error();
+
+// Stream captures (thread-local mode) run in several host threads at once,
+// e.g. one per served request.  Device and pinned allocations and frees
+// synchronize the device, which would break a capture in progress, so they
+// take this gate exclusively while captures hold it shared.  Nothing may
+// allocate inside a capture section.
+std::shared_mutex& capture_gate();
+bool& thread_in_capture();
+struct AllocGate {
+    std::unique_lock<std::shared_mutex> lk;
+    AllocGate() : lk(capture_gate(), std::defer_lock)
+    {
+        if (thread_in_capture()) throw std::logic_error("device allocation inside a stream capture");
+        lk.lock();
+    }
+};
+struct CaptureGate {
+    std::shared_lock<std::shared_mutex> lk;
+    CaptureGate() : lk(capture_gate()) { thread_in_capture() = true; }
+    ~CaptureGate() { thread_in_capture() = false; }
+};
+inline cudaError_t gated_malloc(void** p, size_t bytes)
+{
+    AllocGate g;
+    return cudaMalloc(p, bytes);
+}
+inline cudaError_t gated_free(void* p)
+{
+    AllocGate g;
+    return cudaFree(p);
+}
+inline cudaError_t gated_malloc_host(void** p, size_t bytes)
+{
+    AllocGate g;
+    return cudaMallocHost(p, bytes);
+}
+inline cudaError_t gated_free_host(void* p)
+{
+    AllocGate g;
+    return cudaFreeHost(p);
+}
 
 template <class T>
 struct DevArray {
@@ -75,11 +118,11 @@ struct DevArray {
     {
         release();
         n = count;
-        if (count) UNAP_CK(cudaMalloc((void**)&p, count * sizeof(T)));
+        if (count) UNAP_CK(gated_malloc((void**)&p, count * sizeof(T)));
     }
     void release()
     {
-        if (p) cudaFree(p);
+        if (p) gated_free(p);
         p = nullptr;
         n = 0;
     }
