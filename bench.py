@@ -391,6 +391,9 @@ def main():
                     help="only time the finest-level kernels one launch at a time "
                          "(the small case for kernel profiles) and exit")
     ap.add_argument("--reps", type=int, default=5, help="repetitions for --kernels")
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="bracket one extra mixed solve after the timed ones with "
+                         "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--textio", action="store_true",
                     help="only time the LDU text dump printer and reader (host) and exit")
     args = ap.parse_args()
@@ -450,6 +453,12 @@ def main():
     launches = capi.load().unap_cuda_launch_count() - launches0
     clk = clocks.stop()
     barrier(dist, device)
+    if args.profile_solve:
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        solve(G)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     dev_s = [st["seconds"] for st in stats]
     per_solve = max_over_ranks(statistics.mean(dev_s), dist, device)
     iters = stats[-1]["nIterations"]
