@@ -18,6 +18,10 @@ point (unap_cuda_amg_solve_host) with the b/x host<->device copies inside.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c4]
     python bench.py --impl reference      # the CPU reference arm
 
+A 1-GPU run also serves the seeded 200-request stream of config c5
+(`serving`: solves/s and p50/p99 latency beside the one-at-a-time FP64
+path; `--serve 0` skips it).
+
 Multi-GPU runs are independent replicas (one system per rank, no collective
 on the data path); the reported time is the max over ranks.
 """
@@ -383,8 +387,9 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="grid edge scale (testing)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-iters", type=int, default=3)
-    ap.add_argument("--serve", type=int, default=0,
-                    help="also serve this many requests of the c5 stream")
+    ap.add_argument("--serve", type=int, default=200,
+                    help="also serve this many requests of the c5 stream (rank 0 of a "
+                         "1-GPU run; 0: skip)")
     ap.add_argument("--serve-slots", type=int, default=12,
                     help="concurrent large-request slots of the server")
     ap.add_argument("--kernels", action="store_true",
@@ -536,7 +541,7 @@ def main():
                    "sample": f"failed: {e}"}
 
     serving = None
-    if args.serve > 0 and rank == 0:
+    if args.serve > 0 and rank == 0 and world == 1:
         try:
             serving = serve_bench(args.serve, seed=rank, max_slots=args.serve_slots)
         except Exception as e:  # reported in the line, never fatal

@@ -43,11 +43,11 @@ def write_ldu_py(path, s, fmt="{:.15e}"):
     with open(path, "w") as f:
         f.write(f"nCells: {s.n} nnz: {nnz} symm: {1 if s.symm else 0}\n")
         for i in range(s.n):
-            f.write(f"{i} {i} {fmt.format(s.diag[i])}\n")
+            f.write(f"{i} {i} {fmt.format(float(s.diag[i]))}\n")
         for k in range(s.nf):
-            f.write(f"{s.lower_addr[k]} {s.upper_addr[k]} {fmt.format(s.upper[k])} ")
+            f.write(f"{s.lower_addr[k]} {s.upper_addr[k]} {fmt.format(float(s.upper[k]))} ")
             if not s.symm:
-                f.write(fmt.format(s.lower[k]))
+                f.write(fmt.format(float(s.lower[k])))
             f.write("\n")
 
 
@@ -306,3 +306,24 @@ def test_vector_errors(tmp_path):
         capi.read_vector(tmp_path / "missing.txt", 3)
     with pytest.raises(capi.UnapCudaError, match="cannot create"):
         capi.print_vector(np.zeros(2), tmp_path / "no_such_dir" / "v")
+
+
+@pytest.mark.gpu
+def test_text_dump_to_device_solve(cuda, orc, tmp_path):
+    """A matrix and right-hand side read from the reference's text dumps
+    solve on the device like the same system given as arrays."""
+    torch = cuda
+    s = W.lognormal(14, 12, 10, seed=31, permute=True)
+    write_ldu_py(tmp_path / "A.txt", s, fmt="{!r}")
+    with open(tmp_path / "b.txt", "w") as f:
+        f.write(f"nCells: {s.n}\n" + "".join(f"{float(v)!r}\n" for v in s.b))
+    h = capi.read_ldu_matrix(tmp_path / "A.txt")
+    b = capi.read_vector(tmp_path / "b.txt", s.n)
+    m = capi.handle_ldu(h)
+    # Python's repr round-trips exactly, so the arrays are the system's own
+    assert _same(m["upper"], s.upper) and _same(m["diag"], s.diag) and _same(b, s.b)
+    # pcgsolversolve_ deletes the handle, like the reference's
+    x, n_iter, _ = capi.pcgsolversolve(np.zeros(s.n), h, b, 2, rel_tol=1e-9)
+    x_ref, st_ref = orc.pcg(s, 2, s.b, rel_tol=1e-9)
+    assert abs(n_iter - st_ref["n_iter"]) <= 1
+    assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
