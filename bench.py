@@ -377,6 +377,47 @@ def textio_case(args):
     print(json.dumps(out), flush=True)
 
 
+def setup_case(args):
+    """Setup of the workload's matrix and mixed AMG hierarchy, built by the
+    device kernels (the default) and by the host loops, wall-clock timed
+    with the device synchronized; the two must give the same internal order
+    and hierarchy."""
+    import torch
+    from unap_gb300 import capi
+    from unap_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    s = W.config(args.workload, args.scale, seed=0)
+    wl = WORKLOADS[args.workload]
+    out = {"mode": "setup", "workload": args.workload, "scale": args.scale, "cells": s.n,
+           "faces": s.nf}
+    layouts = {}
+    for name, min_cells in (("device", 32768), ("host", -1)):
+        old = capi.set_device_setup(min_cells)
+        try:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            A = capi.DeviceMatrix(s)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            G = capi.DeviceAmg(A, precision=wl["precision"], rel_tol=1e-10, n_coarsest=1000)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+        finally:
+            capi.set_device_setup(old)
+        info = G.info()
+        layouts[name] = (A.layout()[0], info["cells"])
+        out[name] = {"matrix_s": t1 - t0, "amg_s": t2 - t1, "levels": info["n_levels"]}
+        G.close()
+        A.close()
+    out["same_order_and_hierarchy"] = bool(
+        np.array_equal(layouts["device"][0], layouts["host"][0])
+        and layouts["device"][1] == layouts["host"][1])
+    out["speedup"] = ((out["host"]["matrix_s"] + out["host"]["amg_s"])
+                      / (out["device"]["matrix_s"] + out["device"]["amg_s"]))
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -399,11 +440,16 @@ def main():
     ap.add_argument("--profile-solve", action="store_true",
                     help="bracket one extra mixed solve after the timed ones with "
                          "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
+    ap.add_argument("--setup", action="store_true",
+                    help="only time the matrix and hierarchy setup, device vs host, and exit")
     ap.add_argument("--textio", action="store_true",
                     help="only time the LDU text dump printer and reader (host) and exit")
     args = ap.parse_args()
     if args.textio:
         textio_case(args)
+        return
+    if args.setup:
+        setup_case(args)
         return
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

@@ -2,9 +2,11 @@
 values) against the host build, which is the specification: the same cell
 order and wavefront boundaries exactly, and therefore the same bits from
 every kernel and solve.  Covers many BFS levels (an unpermuted grid), several
-connected components with runs of isolated cells, asymmetric values, a cell
-with more lower neighbours than the device build takes (declined to the host,
-same result), and AMG hierarchies whose coarse levels carry locality keys.
+connected components with runs of isolated cells, asymmetric values, and
+AMG hierarchies whose coarse levels carry locality keys; shapes the device
+build declines go to the host with the same result (a cell with more lower
+neighbours than it takes, a chain with more wavefronts, more connected
+components than it follows).
 """
 import numpy as np
 import pytest
@@ -60,8 +62,21 @@ def star(n_leaves=1500, seed=0):
     return W.LduSystem(n, l, u, None, diag, up, rng.standard_normal(n), name="star")
 
 
+def chain(n=6000, seed=0):
+    """A 1-D chain in natural order: n wavefronts, more than the device
+    build takes (declined to the host, same result)."""
+    rng = np.random.default_rng(seed)
+    l = np.arange(n - 1, dtype=np.int32)
+    u = l + 1
+    up = -rng.random(n - 1) - 0.5
+    diag = np.full(n, 3.0)
+    return W.LduSystem(n, l, u, None, diag, up, rng.standard_normal(n), name="chain")
+
+
 def systems():
-    return [W.lognormal(20, 18, 16, seed=3, permute=True),
+    return [chain(),
+            merged([W.laplace(3, 2, 2, seed=40 + k, permute=True) for k in range(70)], seed=2),
+            W.lognormal(20, 18, 16, seed=3, permute=True),
             W.laplace(24, 20, 18, seed=4, permute=False),     # 60 wavefronts, deep BFS
             W.convdiff(16, 14, 12, seed=2, permute=True),     # asymmetric
             merged([W.laplace(9, 8, 7, seed=5, permute=True),
