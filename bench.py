@@ -394,8 +394,11 @@ def setup_case(args):
     layouts = {}
     for name, min_cells in (("device", 32768), ("host", -1)):
         old = capi.set_device_setup(min_cells)
+        bracket = args.profile_solve and name == "device"
         try:
             torch.cuda.synchronize()
+            if bracket:
+                torch.cuda.profiler.start()
             t0 = time.perf_counter()
             A = capi.DeviceMatrix(s)
             torch.cuda.synchronize()
@@ -403,6 +406,8 @@ def setup_case(args):
             G = capi.DeviceAmg(A, precision=wl["precision"], rel_tol=1e-10, n_coarsest=1000)
             torch.cuda.synchronize()
             t2 = time.perf_counter()
+            if bracket:
+                torch.cuda.profiler.stop()
         finally:
             capi.set_device_setup(old)
         info = G.info()
@@ -438,8 +443,9 @@ def main():
                          "(the small case for kernel profiles) and exit")
     ap.add_argument("--reps", type=int, default=5, help="repetitions for --kernels")
     ap.add_argument("--profile-solve", action="store_true",
-                    help="bracket one extra mixed solve after the timed ones with "
-                         "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
+                    help="bracket one extra mixed solve after the timed ones (with --setup: "
+                         "the device setup) with cudaProfilerStart/Stop, for ncu "
+                         "--profile-from-start off")
     ap.add_argument("--setup", action="store_true",
                     help="only time the matrix and hierarchy setup, device vs host, and exit")
     ap.add_argument("--textio", action="store_true",
