@@ -368,7 +368,7 @@ int unap_cuda_set_packed_sweeps(int mode);
  * levels with at most singleRows rows run on the cluster's first CTA alone.
  * tailRows = 0 launches one kernel per wavefront on every level.  The
  * V-cycle result is bit-identical either way.  Defaults: FP64 2097152 and
- * 8192, FP32 0 (off) and 2^30; the previous values are returned through the
+ * 8192, FP32 8192 and 8192; the previous values are returned through the
  * (nullable) pointers.  Applies to V-cycles launched after the call, CUDA
  * graphs captured before keep their launches.  No counterpart in the
  * reference. */

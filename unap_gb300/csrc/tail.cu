@@ -25,8 +25,8 @@ namespace {
 // is off; FP64 launches are slower and the tail still wins from ~100k rows
 std::atomic<int> g_packedSweeps{1};
 
-std::atomic<long long> g_tailRows[2] = {{1ll << 21}, {0}};
-std::atomic<long long> g_singleRows[2] = {{8192}, {1ll << 30}};
+std::atomic<long long> g_tailRows[2] = {{1ll << 21}, {8192}};
+std::atomic<long long> g_singleRows[2] = {{8192}, {8192}};
 
 constexpr int kStaticSmem =
     kTailMaxWaves * 4 + kTailMaxCluster * 4 + kTailMaxLevels * (int)sizeof(TailLevel) + 64;
