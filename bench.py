@@ -584,6 +584,30 @@ def main():
                 "algorithmic_bytes_per_sweep": sweep_bytes, "sweep_ms": sweep_ms,
                 "peak_source": peak_src, "spmv64": spmv, "whole_solve": whole}
 
+    # the kernels with the largest share of device time: the V-cycle's
+    # sweeps on levels 1..L-1 (row-packed, one launch per wavefront; the
+    # smallest levels run in the one-CTA tail), from the per-level profile
+    # of a graph-captured V-cycle; algorithmic bytes per level = 4 sweeps and
+    # one residual of (16 N + 12 F) for FP32 rows (8 x 4 bytes for FP64)
+    prof = G.profile_vcycle(reps=10)
+    lsz = G.level_sizes()
+    lvl_ms = prof["level_ms"]
+    cb, fb = (16.0, 12.0) if mixed else (32.0, 16.0)
+    coarse_bytes = sum(5 * (cb * n + fb * f) for (n, f, _) in lsz[1:-1])
+    coarse_ms = sum(lvl_ms[1:len(lsz) - 1]) + (lvl_ms[len(lsz) - 1] if len(lvl_ms) >= len(lsz)
+                                               else 0.0)
+    coarse_gbs = coarse_bytes / (coarse_ms * 1e-3) / 1e9 if coarse_ms > 0 else None
+    roofline["coarse_levels"] = {
+        "kernel": "gs_packed_kernel<float>" if mixed else "gs_packed_kernel<double>",
+        "levels": f"1-{len(lsz) - 1} (with the coarsest dense solve)",
+        "share_of_vcycle": coarse_ms / prof["vcycle_ms"] if prof["vcycle_ms"] else None,
+        "vcycle_ms": prof["vcycle_ms"], "level_ms": lvl_ms[:len(lsz)],
+        "wavefronts_per_level": [w for (_, _, w) in lsz],
+        "algorithmic_bytes": coarse_bytes, "ms": coarse_ms,
+        "achieved": coarse_gbs, "unit": "GB/s",
+        "frac": coarse_gbs / peak if coarse_gbs else None,
+        "bound": "latency: one dependent launch per wavefront (about 2,000 per V-cycle)"}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:

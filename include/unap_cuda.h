@@ -234,10 +234,10 @@ void unap_cuda_amg_default_params(unap_cuda_amg_params* p);
 /* builds the hierarchy of an existing matrix handle (the matrix must outlive
  * the AMG handle) */
 int unap_cuda_amg_create(long int* amg, long int matrix, const unap_cuda_amg_params* p);
-/* Internal cell order of AMG level `level` (0 = the matrix), as
- * unap_cuda_matrix_layout gives it. */
-int unap_cuda_amg_level_layout(long int amg, int level, int* nCells, int* nWavefronts, int* perm,
-                               int* waveStart);
+/* Size (cells, faces) and internal cell order of AMG level `level` (0 =
+ * the matrix), the order as unap_cuda_matrix_layout gives it. */
+int unap_cuda_amg_level_layout(long int amg, int level, int* nCells, long long* nFaces,
+                               int* nWavefronts, int* perm, int* waveStart);
 /* nLevels including the finest; cells[k] for k < min(nLevels, maxOut) */
 int unap_cuda_amg_info(long int amg, int* nLevels, int* cells, int* wavefronts, int maxOut,
                        double* setupSeconds, long long* deviceBytes);

@@ -124,7 +124,8 @@ SIGNATURES = {
     "unap_cuda_server_destroy": (_c_int, [_c_long]),
     "unap_cuda_set_device_setup": (_c_int, [_c_ll, ctypes.POINTER(_c_ll)]),
     "unap_cuda_matrix_layout": (_c_int, [_c_long, _ip, _vp, _vp]),
-    "unap_cuda_amg_level_layout": (_c_int, [_c_long, _c_int, _ip, _ip, _vp, _vp]),
+    "unap_cuda_amg_level_layout": (_c_int, [_c_long, _c_int, _ip, ctypes.POINTER(_c_ll), _ip,
+                                            _vp, _vp]),
     "unap_cuda_read_ldu_matrix": (_c_int, [ctypes.c_char_p, _lp]),
     "unap_cuda_read_vector": (_c_int, [ctypes.c_char_p, _c_ll, _vp]),
     "unap_cuda_read_interfaces": (_c_int, [ctypes.c_char_p, _ip, ctypes.POINTER(_c_ll), _vp, _vp,
@@ -343,10 +344,11 @@ def _layout(fn, *head):
                                           ws.ctypes.data))
         return perm, ws
     lib = load()
-    check(lib.unap_cuda_amg_level_layout(*head, ctypes.byref(n), ctypes.byref(nw), None, None))
+    check(lib.unap_cuda_amg_level_layout(*head, ctypes.byref(n), None, ctypes.byref(nw), None,
+                                         None))
     perm = np.zeros(n.value, np.int32)
     ws = np.zeros(nw.value + 1, np.int32)
-    check(lib.unap_cuda_amg_level_layout(*head, ctypes.byref(n), ctypes.byref(nw),
+    check(lib.unap_cuda_amg_level_layout(*head, ctypes.byref(n), None, ctypes.byref(nw),
                                          perm.ctypes.data, ws.ctypes.data))
     return perm, ws
 
@@ -397,6 +399,17 @@ class DeviceAmg:
     def level_layout(self, level: int):
         """(perm, waveStart) of AMG level `level` (0 = the matrix)."""
         return _layout("unap_cuda_amg_level_layout", self.handle, level)
+
+    def level_sizes(self):
+        """[(cells, faces, wavefronts)] of every level, finest first."""
+        lib = load()
+        out = []
+        for k in range(self.info()["n_levels"]):
+            n, nw, nf = _c_int(), _c_int(), _c_ll()
+            check(lib.unap_cuda_amg_level_layout(self.handle, k, ctypes.byref(n), ctypes.byref(nf),
+                                                 ctypes.byref(nw), None, None))
+            out.append((n.value, nf.value, nw.value))
+        return out
 
     def vcycle(self, r, z):
         check(load().unap_cuda_amg_vcycle(self.handle, _ptr(r), _ptr(z)))

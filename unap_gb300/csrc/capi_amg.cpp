@@ -115,14 +115,15 @@ int unap_cuda_amg_create(long int* amg, long int matrix, const unap_cuda_amg_par
     });
 }
 
-int unap_cuda_amg_level_layout(long int amg, int level, int* nCells, int* nWavefronts, int* perm,
-                               int* waveStart)
+int unap_cuda_amg_level_layout(long int amg, int level, int* nCells, long long* nFaces,
+                               int* nWavefronts, int* perm, int* waveStart)
 {
     return guarded([&] {
         AmgHandle* h = amg_from(amg);
         if (level < 0 || level >= h->H->nLevels()) throw std::invalid_argument("no such level");
         const Level& L = *h->H->lv[(size_t)level].L;
         if (nCells) *nCells = L.n;
+        if (nFaces) *nFaces = L.nf;
         if (nWavefronts) *nWavefronts = L.nWave;
         if (perm) std::memcpy(perm, L.perm.data(), sizeof(int) * L.perm.size());
         if (waveStart) std::memcpy(waveStart, L.waveStart.data(), sizeof(int) * L.waveStart.size());
