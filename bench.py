@@ -50,7 +50,7 @@ WORKLOADS = {
 L2_BYTES = 129 * 2 ** 20
 # DRAM bytes / algorithmic bytes of a whole FP32 Gauss-Seidel sweep, measured
 # in situ (no cache flush) with ncu on the 192^3 log-normal matrix
-SWEEP_TRAFFIC_RATIO = 1.32
+SWEEP_TRAFFIC_RATIO = 1.29
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -576,7 +576,7 @@ def main():
                 "traffic": SWEEP_TRAFFIC_RATIO * sweep_bytes if mixed else None,
                 "traffic_source": "in-situ DRAM bytes of a whole FP32 sweep measured by ncu "
                                   "on the 192^3 case (profiles/gs_kernel_float_c4_192cube_"
-                                  "waves.md), ratio 1.32 to algorithmic, scaled to this sweep"
+                                  "waves.md), ratio 1.29 to algorithmic, scaled to this sweep"
                                   if mixed else None,
                 "kernel": "gs_kernel<float>" if mixed else "gs_kernel<double>",
                 "launch_group": f"one forward sweep of the finest level "
