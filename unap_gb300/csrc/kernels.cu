@@ -173,9 +173,9 @@ static void launch_gs(const Exec& ex, const Rows<T>& A, T* x, const T* b, int r0
     cudaLaunchConfig_t cfg = {};
     // one row per thread (every row's matrix data is loaded before the
     // dependency wait), or a grid-stride loop over at most maxBlocks CTAs;
-    // wavefronts of up to 100,000 rows go out in CTAs of 64 threads, spread
-    // over four times as many SMs (latency-bound, as gs_sweep_packed)
-    const int threads = g_rowGrid.load() && r1 - r0 <= 100000 ? 64 : kBlock;
+    // wavefronts of up to 100,000 rows go out in CTAs of one warp, spread
+    // over eight times as many SMs (latency-bound, as gs_sweep_packed)
+    const int threads = g_rowGrid.load() && r1 - r0 <= 100000 ? 32 : kBlock;
     const long long need = div_up(r1 - r0, threads);
     cfg.gridDim = dim3((unsigned)(g_rowGrid.load() ? std::max(1LL, need) : ex.grid(r1 - r0)));
     cfg.blockDim = dim3(threads);

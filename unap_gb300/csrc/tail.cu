@@ -747,11 +747,12 @@ void gs_sweep_packed(const Exec& ex, const Level& L, const PackedRows& P, const 
         const int w = backward ? W - 1 - k : k;
         const int r0 = L.waveStart[(size_t)w], r1 = L.waveStart[(size_t)w + 1];
         if (r1 <= r0) continue;
-        // a wavefront of up to kSmallWaveRows rows in CTAs of 64 threads is
-        // spread over four times as many SMs as with 256: each SM then
-        // carries fewer rows' loads and gathers, so the latency-bound
-        // wavefront ends sooner (256^3 FP32 V-cycle 10.14 -> 9.38 ms)
-        const int threads = (r1 - r0) <= kSmallWaveRows ? 64 : kBlock;
+        // a wavefront of up to kSmallWaveRows rows in CTAs of one warp is
+        // spread over eight times as many SMs as with 256 threads: each SM
+        // then carries fewer rows' loads and gathers, so the latency-bound
+        // wavefront ends sooner (256^3 FP32 V-cycle 10.14 ms with 256,
+        // 9.38 ms with 64, 9.27 ms with 32 threads per CTA)
+        const int threads = (r1 - r0) <= kSmallWaveRows ? 32 : kBlock;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)div_up(r1 - r0, threads));
         cfg.blockDim = dim3(threads);
