@@ -104,3 +104,37 @@ def test_bad_handle_is_an_error_not_a_crash():
     assert b"invalid matrix handle" in lib.unap_cuda_last_error()
     with pytest.raises(capi.UnapCudaError):
         capi.handle_ldu(bogus.ctypes.data)
+
+
+def test_coo_ingest_rejects_what_the_reference_leaves_undefined():
+    """Host form (small matrices stay on the host): rows out of order, a
+    repeated entry and a column whose lower entries do not match the row's
+    upper ones are errors; the row-sorted input with shuffled columns is
+    the system itself."""
+    from unap_gb300 import workloads as W
+    rng = np.random.default_rng(5)
+    s = W.convdiff(6, 5, 4, seed=2, permute=True)
+    rows = np.concatenate([np.arange(s.n), s.lower_addr, s.upper_addr])
+    cols = np.concatenate([np.arange(s.n), s.upper_addr, s.lower_addr])
+    vals = np.concatenate([s.diag, s.upper, s.lower])
+    o = np.lexsort((rng.random(rows.shape[0]), rows))
+    v, r, c = vals[o], rows[o].astype(np.int32), cols[o].astype(np.int32)
+    h = capi.coo2ldumatrixcreat(v, r + 1, c + 1, s.n, symm=False)
+    m = capi.handle_ldu(h)
+    capi.sw_matrix_destroy(h)
+    assert np.array_equal(m["upper_addr"], s.upper_addr) and np.array_equal(m["lower"], s.lower)
+    lower = np.nonzero(c < r)[0]
+    upper = np.nonzero(c > r)[0]
+    k = lower[len(lower) // 2]
+    taken = set(c[r == r[k]].tolist())
+    c_bad = c.copy()
+    c_bad[k] = next(x for x in range(int(r[k])) if x not in taken)
+    r_bad = r.copy()
+    r_bad[[upper[3], upper[-3]]] = r_bad[[upper[-3], upper[3]]]
+    c_dup = c.copy()
+    row = np.nonzero(r == r[upper[5]])[0]
+    c_dup[row[0]] = c_dup[row[1]]
+    for cc, rr, msg in ((c_bad, r, "structurally symmetric"), (c, r_bad, "ascending row order"),
+                        (c_dup, r, "repeats an entry")):
+        with pytest.raises(capi.UnapCudaError, match=msg):
+            capi.coo2ldumatrixcreat(v, rr + 1, cc + 1, s.n, symm=False)
