@@ -138,3 +138,43 @@ def test_coo_ingest_rejects_what_the_reference_leaves_undefined():
                         (c_dup, r, "repeats an entry")):
         with pytest.raises(capi.UnapCudaError, match=msg):
             capi.coo2ldumatrixcreat(v, rr + 1, cc + 1, s.n, symm=False)
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """include/unap_cuda.h compiles as C99 with warnings as errors, and a C
+    program calling entry points from both parts links against the library
+    (what a Fortran/C caller of the reference relinks to)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    lib = build.build()
+    src = tmp_path / "caller.c"
+    src.write_text(r'''
+#include "unap_cuda.h"
+#include <stdio.h>
+int main(void)
+{
+    long int A = 0;
+    int n = 2, nf = 1, l = 0, u = 1;
+    double diag[2] = {2.0, 2.0}, upper = -1.0;
+    /* lower == upper: symmetric, the reference's convention */
+    ldumatrixcreat_(&A, &n, &nf, &l, &u, &upper, diag, &upper);
+    int cells = 0, faces = 0, symm = 0;
+    if (unap_cuda_matrix_size(A, &cells, &faces, &symm) != 0) return 1;
+    sw_matrix_destroy__(&A);
+    printf("%s %d %d %d\n", unap_cuda_version(), cells, faces, symm);
+    return cells == 2 && faces == 1 && symm == 1 ? 0 : 2;
+}
+''')
+    exe = tmp_path / "caller"
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                        "-I", os.path.join(ROOT, "include"), str(src), lib,
+                        "-Wl,-rpath," + os.path.dirname(lib), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    # host-only calls: no GPU needed to run it
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, (run.stdout, run.stderr)
+    assert "sm_103a" in run.stdout
