@@ -302,8 +302,8 @@ __global__ void k_bfs_assign(Adj A, const int* __restrict__ F, int m, const int*
     }
 }
 
-// smallest cell >= from that is unvisited (and, if needIso >= 0, whose
-// isolation matches: needIso 0 = has a neighbour)
+// smallest cell >= from that is unvisited (with needNbr != 0: and has at
+// least one neighbour), atomically minimised into *best
 __global__ void k_first_unvisited(Adj A, int from, int n, const int* rank, int needNbr, int* best)
 {
     for (long long c = from + blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
