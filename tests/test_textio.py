@@ -353,3 +353,34 @@ def test_golden_fixtures_from_the_reference_printer(tmp_path):
     m = capi.handle_ldu(h2)
     capi.sw_matrix_destroy(h2)
     assert m["n"] == 36 and not m["symm"]
+
+
+def test_random_numeric_fields_read_like_the_reference(R, tmp_path):
+    """Thousands of numeric fields in random spellings (fixed, scientific
+    and shortest forms, signs, leading zeros, upper-case exponents, many or
+    few digits, subnormal and huge magnitudes) read bit for bit like the
+    reference reader."""
+    rng = np.random.default_rng(99)
+    out = []
+    for _ in range(4000):
+        m = rng.standard_normal() * 10.0 ** rng.integers(-320, 309)
+        kind = rng.integers(0, 7)
+        if kind == 0:
+            t = repr(float(m))
+        elif kind == 1:
+            t = f"{m:.{rng.integers(0, 25)}e}"
+        elif kind == 2:
+            t = f"{m:.{rng.integers(1, 20)}g}"
+        elif kind == 3:
+            t = f"{m:.{rng.integers(0, 12)}E}"
+        elif kind == 4:
+            t = f"{rng.integers(-10**12, 10**12)}"
+        elif kind == 5:
+            t = "+" + f"{abs(m):.17e}"
+        else:
+            digits = "".join(str(d) for d in rng.integers(0, 10, rng.integers(1, 40)))
+            t = f"{'-' if rng.random() < 0.5 else ''}00{digits[:5]}.{digits[5:]}e{rng.integers(-330, 330)}"
+        out.append(t)
+    p = tmp_path / "fuzz.txt"
+    p.write_text(f"nCells: {len(out)}\n" + "\n".join(out) + "\n")
+    assert _same(capi.read_vector(p, len(out)), R.read_vector(p, len(out)))
