@@ -1443,6 +1443,12 @@ static void amg_prec_cb(void* ctx, const double* r, double* w) { orc_amg_vcycle(
 
 /* PCG.cpp:35-183 with the V-cycle as preconditioner.  flexible: beta =
  * z_k.(r_k - r_{k-1}) / z_{k-1}.r_{k-1}, using r_{k-1} = r_k + alpha q. */
+/* Bench helper (reference arm): the iteration cap of later solves. */
+void orc_amg_set_max_iter(void* hv, int maxIter)
+{
+    ((oamg*)hv)->p.maxIter = maxIter;
+}
+
 void orc_amg_pcg(void* hv, double* x, const double* b, int* nIter, double* initRes,
                  double* finalRes, double* trueRes, int* converged)
 {

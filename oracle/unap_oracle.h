@@ -99,6 +99,7 @@ void orc_amg_pcg(void* h, double* x, const double* b, int* nIter, double* initRe
 /* dense inverse of the coarsest matrix, row-major n x n (FP64) */
 void orc_amg_coarse_inverse(void* h, double* inv);
 void orc_amg_destroy(void* h);
+void orc_amg_set_max_iter(void* h, int maxIter);
 
 /* Cholesky-based inverse of a dense SPD matrix (row-major), as used for the
  * coarsest level.  Returns 0 on success, -1 when not positive definite. */

@@ -269,6 +269,9 @@ class OracleAmg:
         return x, dict(n_iter=it.value, init_res=ir.value, final_res=fr.value,
                        true_res=tr.value, converged=bool(cv.value))
 
+    def set_max_iter(self, k: int) -> None:
+        self.lib.orc_amg_set_max_iter(self.h, _c_int(k))
+
     def close(self):
         if self.h:
             self.lib.orc_amg_destroy(self.h)
