@@ -149,3 +149,22 @@ def test_amg_pcg_oracle_converges(orc):
         inv = A.coarse_inverse()
         assert np.allclose(inv, inv.T, rtol=0, atol=0)
         A.close()
+
+
+def test_amg_iteration_cap_can_change(orc):
+    """The reference arm's sampling: one hierarchy, solves capped at 1, 6
+    and then unlimited iterations; the capped runs restart from x = 0 and
+    the residuals decrease with the cap."""
+    from oracle_lib import OracleAmg
+    s = W.lognormal(12, seed=4)
+    A = OracleAmg(orc, s, n_coarsest=60, precision=0, rel_tol=1e-10, max_iter=1)
+    _, s1 = A.solve(s.b)
+    A.set_max_iter(6)
+    _, s6 = A.solve(s.b)
+    A.set_max_iter(500)
+    _, sf = A.solve(s.b)
+    assert (s1["n_iter"], s6["n_iter"]) == (1, 6)
+    assert s1["init_res"] == s6["init_res"] == sf["init_res"]
+    assert sf["converged"] and sf["n_iter"] > 6
+    assert s1["final_res"] > s6["final_res"] > sf["final_res"]
+    A.close()
