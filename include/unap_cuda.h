@@ -216,18 +216,32 @@ int unap_cuda_krylov_solve(long int handle, int method, int precond, double tol,
  * b - A x, recursion, injection, nPostSweeps backward sweeps; the coarsest
  * level is solved with a dense FP64 Cholesky-based inverse.  precision 1
  * runs the whole V-cycle in FP32 inside the FP64 PCG (true residual, dot
- * products, norms and the coarsest product stay FP64). */
+ * products, norms and the coarsest product stay FP64).
+ *
+ * smoother 1 smooths the levels from chebyFrom down (Gauss-Seidel above)
+ * with the reference's Chebyshev iteration (chebySmoother.cpp:44-148) of
+ * degree chebyDegree before and after the coarse correction, over
+ * [lambda / eigRatio, 1.1 lambda]; lambda is the reference's
+ * diagonal-PCG + Lanczos estimate (eigenDiagPCG.cpp:11-361) of each level's
+ * largest eigenvalue of D^-1 A, taken once at setup from x = 0 (the
+ * reference's smoother estimates on its first call and leaves x changed by
+ * it, which a fixed PCG preconditioner cannot do).  eigRatio <= 0 selects
+ * the reference's 1.5. */
 typedef struct {
     int nCoarsest;   /* default 1000 */
     int maxLevels;   /* default 50 */
-    int nPreSweeps;  /* default 2 */
-    int nPostSweeps; /* default 2 */
+    int nPreSweeps;  /* default 2 (Gauss-Seidel levels) */
+    int nPostSweeps; /* default 2 (Gauss-Seidel levels) */
     int precision;   /* 0 FP64 V-cycle, 1 FP32 V-cycle */
     int flexible;    /* 1: Polak-Ribiere beta (default 1 when precision 1) */
     double tol;      /* default 0 */
     double relTol;   /* default 1e-10 */
     int maxIter;     /* default 500 */
     int minIter;     /* default 0 */
+    int smoother;    /* 0 Gauss-Seidel (default), 1 Chebyshev */
+    int chebyDegree; /* default 3 (1..16) */
+    int chebyFrom;   /* first Chebyshev level, default 0 (all) */
+    double eigRatio; /* default 30 */
 } unap_cuda_amg_params;
 
 void unap_cuda_amg_default_params(unap_cuda_amg_params* p);
@@ -250,6 +264,10 @@ int unap_cuda_amg_vcycle(long int amg, const double* r, double* z);
  * the levels below it 0).  *written = entries filled.  No counterpart in the
  * reference. */
 int unap_cuda_amg_profile_vcycle(long int amg, int reps, double* ms, int maxOut, int* written);
+/* The Chebyshev smoother's eigenvalue estimate of every level but the
+ * coarsest (0 on Gauss-Seidel levels): lam[k] for k < min(nLevels - 1,
+ * maxOut); *written = entries filled.  No counterpart in the reference. */
+int unap_cuda_amg_eigenvalues(long int amg, double* lam, int maxOut, int* written);
 /* AMG-PCG on device vectors (x holds the initial guess) */
 int unap_cuda_amg_solve(long int amg, double* x, const double* b, unap_cuda_stats* stats);
 /* AMG-PCG on host vectors: copies b and x in, solves, copies x out */
@@ -359,6 +377,12 @@ int unap_cuda_set_wave_grid(int oneRowPerThread);
  * identical.  Returns the previous setting.  No counterpart in the
  * reference. */
 int unap_cuda_set_packed_sweeps(int mode);
+
+/* Chebyshev-step launches (AMG V-cycle with smoother 1) on levels of at
+ * most `rows` rows use one-warp CTAs, spread over more SMs than 256-thread
+ * CTAs would be (default 100000).  Results are identical.  Returns the
+ * previous setting.  No counterpart in the reference. */
+int unap_cuda_set_cheby_small_rows(int rows);
 
 /* Coarse-level tail of the AMG V-cycle (per-step executor), set for the FP64
  * (precision 0) or FP32 (precision 1) V-cycle: every level with at most

@@ -1228,6 +1228,22 @@ int orc_dense_spd_inverse(int n, const double* A, double* inv)
  *                 in ascending column order from 0.
  * precision 1 runs every level matrix, vector and sweep in FP32 (values
  * rounded from FP64), with the coarsest product in FP64.
+ *
+ * smoother 1 replaces the sweeps of levels k >= chebyFrom by the reference's
+ * Chebyshev iteration (chebySmoother.cpp:44-148) of degree chebyDegree
+ * before and after the coarse correction:
+ *   from x = 0:   w = rD b Rtheta;  x = w
+ *   from x != 0:  w = rD (b - A x) Rtheta;  x += w
+ *   step j >= 1:  w = d1_j w + d2_j rD (b - A x);  x += w
+ * rD = 1 / diag, A x in the reference SpMV order, the coefficients from the
+ * level's eigenvalue estimate lambda as in chebySmoother.cpp:62-108 with
+ * [lambda / eigRatio, 1.1 lambda].  lambda is estimated once at setup by
+ * the reference's diagonal-PCG + Lanczos + Sturm bisection
+ * (eigenDiagPCG.cpp:11-361) from x = 0 and b = orc_eig_start, on the FP64
+ * level matrix; the same polynomial before and after keeps the V-cycle
+ * symmetric, so it stays a fixed PCG preconditioner (the reference's first
+ * call, which only estimates and leaves x changed, would not be).  FP32
+ * levels use rD = 1.0f / diag32 and the coefficients rounded to float.
  * --------------------------------------------------------------------- */
 typedef struct {
     int n, nf;
@@ -1241,6 +1257,7 @@ typedef struct {
 typedef struct {
     ohier* h;
     orc_amg_params p;
+    double* lam;       /* per smoothed level: eigenvalue estimate (Chebyshev) */
     int nLv;           /* total levels incl. fine */
     const omat** A;    /* per level FP64 view */
     fmat* F;           /* per level FP32 copy (precision 1) */
@@ -1306,6 +1323,158 @@ static void fspmv(const fmat* m, const float* x, float* y)
 
 static const int* amg_restrict_map(oamg* g, int k) { return g->h->lv[k].restrictAddr; }
 
+/* splitmix64 (Steele, Lea, Flood 2014), the start vector's hash */
+double orc_eig_start(long long c)
+{
+    unsigned long long z = (unsigned long long)c + 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+}
+
+/* Chebyshev coefficients, chebySmoother.cpp:62-108: Rtheta for the first
+ * step and (d1, d2) of steps 1..deg-1 */
+static void amg_cheb_coeffs(double lam, double ratio, int deg, double* Rtheta, double* d1,
+                            double* d2)
+{
+    double maxEig = lam * 1.1;
+    double minEig = lam / ratio;
+    double delta = 2.0 / (maxEig - minEig);
+    double theta = 0.5 * (maxEig + minEig);
+    double s1 = theta * delta;
+    double rhok = 1.0 / s1;
+    *Rtheta = 1.0 / theta;
+    for (int k = 1; k < deg; ++k) {
+        double rhokp1 = 1.0 / (2.0 * s1 - rhok);
+        d1[k] = rhokp1 * rhok;
+        d2[k] = 2.0 * rhokp1 * delta;
+        rhok = rhokp1;
+    }
+}
+
+#define AMG_MAX_DEGREE 16
+
+static int amg_is_cheby(const oamg* g, int k)
+{
+    return g->p.smoother == 1 && k >= g->p.chebyFrom;
+}
+
+static double amg_ratio(const oamg* g) { return g->p.eigRatio > 0 ? g->p.eigRatio : 1.5; }
+
+/* eigenDiagPCG.cpp:11-361 from x = 0, b = orc_eig_start: a breakdown
+ * (|wArA| < VSMALL) ends the Lanczos matrix at the iterations done */
+static double amg_level_eig(const omat* m)
+{
+    int n = m->n;
+    double* x = (double*)xcalloc((size_t)n, sizeof(double));
+    double* b = (double*)xcalloc((size_t)n, sizeof(double));
+    double* rD = (double*)xcalloc((size_t)n, sizeof(double));
+    double al[10] = {0}, be[10] = {0};
+    for (int c = 0; c < n; ++c) b[c] = orc_eig_start(c);
+    diag_rD(m, rD);
+    diag_pcg_loops(m, x, b, rD, 10, al, be);
+    int nP = 0;
+    while (nP < 10 && al[nP] != 0.0) ++nP;
+    double lam = nP >= 2 ? compute_max_eig(al, be, nP) : (nP == 1 ? 1.0 / al[0] : 1.0);
+    free(x);
+    free(b);
+    free(rD);
+    return lam;
+}
+
+/* the Chebyshev chain of one level in FP64 (w: n-vector scratch) */
+static void cheb_chain64(const omat* A, double lam, double ratio, int deg, double* x,
+                         const double* b, double* w, int fromZero)
+{
+    int n = A->n;
+    double Rth, d1[AMG_MAX_DEGREE], d2[AMG_MAX_DEGREE];
+    amg_cheb_coeffs(lam, ratio, deg, &Rth, d1, d2);
+    double* p = (double*)xcalloc((size_t)n, sizeof(double));
+    if (fromZero) {
+        for (int c = 0; c < n; ++c) {
+            double rD = 1.0 / A->diag[c];
+            double wi = rD * b[c] * Rth;
+            w[c] = wi;
+            x[c] = wi;
+        }
+    } else {
+        mat_spmv(A, x, p);
+        for (int c = 0; c < n; ++c) {
+            double rD = 1.0 / A->diag[c];
+            double wi = rD * (b[c] - p[c]) * Rth;
+            w[c] = wi;
+            x[c] = x[c] + wi;
+        }
+    }
+    for (int j = 1; j < deg; ++j) {
+        mat_spmv(A, x, p);
+        for (int c = 0; c < n; ++c) {
+            double rD = 1.0 / A->diag[c];
+            double wi = d1[j] * w[c] + d2[j] * rD * (b[c] - p[c]);
+            w[c] = wi;
+            x[c] = x[c] + wi;
+        }
+    }
+    free(p);
+}
+
+static void amg_cheby64(oamg* g, int k, double* x, const double* b, int fromZero)
+{
+    cheb_chain64(g->A[k], g->lam[k], amg_ratio(g), g->p.chebyDegree, x, b, g->r[k], fromZero);
+}
+
+void orc_cheby_chain(int n, int nf, const int* l, const int* u, const double* lo,
+                     const double* d, const double* up, int symm, double lam, double ratio,
+                     int degree, double* x, const double* b, int fromZero)
+{
+    omat m = mat_view(n, nf, l, u, lo, d, up, symm);
+    double* w = (double*)xcalloc((size_t)n, sizeof(double));
+    if (degree < 1 || degree > AMG_MAX_DEGREE) degree = 3;
+    cheb_chain64(&m, lam, ratio, degree, x, b, w, fromZero);
+    free(w);
+}
+
+static void fspmv(const fmat* m, const float* x, float* y);
+
+static void amg_cheby32(oamg* g, int k, float* x, const float* b, int fromZero)
+{
+    const fmat* A = &g->F[k];
+    int n = A->n, deg = g->p.chebyDegree;
+    double Rth, d1[AMG_MAX_DEGREE], d2[AMG_MAX_DEGREE];
+    amg_cheb_coeffs(g->lam[k], amg_ratio(g), deg, &Rth, d1, d2);
+    const float Rf = (float)Rth;
+    float* w = g->rf[k];
+    float* p = (float*)xcalloc((size_t)n, sizeof(float));
+    if (fromZero) {
+        for (int c = 0; c < n; ++c) {
+            float rD = 1.0f / A->diag[c];
+            float wi = rD * b[c] * Rf;
+            w[c] = wi;
+            x[c] = wi;
+        }
+    } else {
+        fspmv(A, x, p);
+        for (int c = 0; c < n; ++c) {
+            float rD = 1.0f / A->diag[c];
+            float wi = rD * (b[c] - p[c]) * Rf;
+            w[c] = wi;
+            x[c] = x[c] + wi;
+        }
+    }
+    for (int j = 1; j < deg; ++j) {
+        const float d1f = (float)d1[j], d2f = (float)d2[j];
+        fspmv(A, x, p);
+        for (int c = 0; c < n; ++c) {
+            float rD = 1.0f / A->diag[c];
+            float wi = d1f * w[c] + d2f * rD * (b[c] - p[c]);
+            w[c] = wi;
+            x[c] = x[c] + wi;
+        }
+    }
+    free(p);
+}
+
 static void amg_vcycle64(oamg* g, int k)
 {
     int L = g->nLv - 1;
@@ -1322,15 +1491,23 @@ static void amg_vcycle64(oamg* g, int k)
     }
     omat* A = (omat*)g->A[k];
     int n = A->n;
-    for (int c = 0; c < n; ++c) x[c] = 0.0;
-    if (g->p.nPre > 0) gs_forward(A, x, b, g->p.nPre);
+    const int cheb = amg_is_cheby(g, k);
+    if (cheb) {
+        amg_cheby64(g, k, x, b, 1);
+    } else {
+        for (int c = 0; c < n; ++c) x[c] = 0.0;
+        if (g->p.nPre > 0) gs_forward(A, x, b, g->p.nPre);
+    }
     mat_spmv(A, x, g->r[k]);
     for (int c = 0; c < n; ++c) g->r[k][c] = b[c] - g->r[k][c];
     restrict_field(n, amg_restrict_map(g, k), g->r[k], g->A[k + 1]->n, g->b[k + 1]);
     amg_vcycle64(g, k + 1);
     const int* map = amg_restrict_map(g, k);
     for (int c = 0; c < n; ++c) x[c] += g->x[k + 1][map[c]];
-    if (g->p.nPost > 0) gs_backward(A, x, b, g->p.nPost);
+    if (cheb)
+        amg_cheby64(g, k, x, b, 0);
+    else if (g->p.nPost > 0)
+        gs_backward(A, x, b, g->p.nPost);
 }
 
 static void amg_vcycle32(oamg* g, int k)
@@ -1350,8 +1527,13 @@ static void amg_vcycle32(oamg* g, int k)
     }
     const fmat* A = &g->F[k];
     int n = A->n;
-    for (int c = 0; c < n; ++c) x[c] = 0.0f;
-    for (int s = 0; s < g->p.nPre; ++s) fgs_sweep(A, x, b, 0);
+    const int cheb = amg_is_cheby(g, k);
+    if (cheb) {
+        amg_cheby32(g, k, x, b, 1);
+    } else {
+        for (int c = 0; c < n; ++c) x[c] = 0.0f;
+        for (int s = 0; s < g->p.nPre; ++s) fgs_sweep(A, x, b, 0);
+    }
     float* r = g->rf[k];
     fspmv(A, x, r);
     for (int c = 0; c < n; ++c) r[c] = b[c] - r[c];
@@ -1362,7 +1544,10 @@ static void amg_vcycle32(oamg* g, int k)
     for (int i = 0; i < n; ++i) bc[map[i]] += r[i];
     amg_vcycle32(g, k + 1);
     for (int c = 0; c < n; ++c) x[c] += g->xf[k + 1][map[c]];
-    for (int s = 0; s < g->p.nPost; ++s) fgs_sweep(A, x, b, 1);
+    if (cheb)
+        amg_cheby32(g, k, x, b, 0);
+    else
+        for (int s = 0; s < g->p.nPost; ++s) fgs_sweep(A, x, b, 1);
 }
 
 void* orc_amg_create(int n, int nf, const int* l, const int* u, const double* d,
@@ -1412,7 +1597,25 @@ void* orc_amg_create(int n, int nf, const int* l, const int* u, const double* d,
         g->F = (fmat*)xcalloc((size_t)g->nLv, sizeof(fmat));
         for (int k = 0; k < g->nLv - 1; ++k) fmat_build(&g->F[k], g->A[k]);
     }
+    g->lam = (double*)xcalloc((size_t)g->nLv, sizeof(double));
+    if (g->p.smoother == 1) {
+        if (g->p.chebyDegree < 1 || g->p.chebyDegree > AMG_MAX_DEGREE) g->p.chebyDegree = 3;
+        for (int k = 0; k < g->nLv - 1; ++k)
+            if (amg_is_cheby(g, k)) g->lam[k] = amg_level_eig(g->A[k]);
+    }
     return g;
+}
+
+void orc_amg_eigs(void* hv, double* lam)
+{
+    oamg* g = (oamg*)hv;
+    for (int k = 0; k < g->nLv - 1; ++k) lam[k] = g->lam[k];
+}
+
+void orc_amg_set_eigs(void* hv, const double* lam)
+{
+    oamg* g = (oamg*)hv;
+    for (int k = 0; k < g->nLv - 1; ++k) g->lam[k] = lam[k];
 }
 
 int orc_amg_nlevels(void* hv) { return ((oamg*)hv)->nLv; }
@@ -1547,6 +1750,7 @@ void orc_amg_destroy(void* hv)
     free(g->bf);
     free(g->rf);
     free(g->Ainv);
+    free(g->lam);
     free((void*)g->A);
     hier_free(g->h);
     free(g);

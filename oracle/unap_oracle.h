@@ -84,6 +84,15 @@ typedef struct {
     int flexible;      /* 1: Polak-Ribiere beta (flexible PCG) */
     double tol, relTol;
     int maxIter, minIter;
+    /* smoother 0: Gauss-Seidel (nPre forward / nPost backward sweeps);
+     * smoother 1: Chebyshev of degree chebyDegree before and after the
+     * coarse correction on levels >= chebyFrom (Gauss-Seidel below), over
+     * [lambda / eigRatio, 1.1 lambda] (chebySmoother.cpp:44-148) with lambda
+     * the level's diagonal-PCG estimate (eigenDiagPCG.cpp:11-361) taken once
+     * at setup from x = 0 and the start vector orc_eig_start.  eigRatio <= 0
+     * means the reference's 1.5. */
+    int smoother, chebyDegree, chebyFrom;
+    double eigRatio;
 } orc_amg_params;
 
 void* orc_amg_create(int n, int nf, const int* l, const int* u, const double* d,
@@ -100,6 +109,20 @@ void orc_amg_pcg(void* h, double* x, const double* b, int* nIter, double* initRe
 void orc_amg_coarse_inverse(void* h, double* inv);
 void orc_amg_destroy(void* h);
 void orc_amg_set_max_iter(void* h, int maxIter);
+/* per-level largest-eigenvalue estimates of D^-1 A used by the Chebyshev
+ * smoother (levels 0..nLevels-2; 0 where the level uses Gauss-Seidel);
+ * set_eigs replaces them (a test feeds the device's estimates back so the
+ * two V-cycles can be compared bit for bit) */
+void orc_amg_eigs(void* h, double* lam);
+void orc_amg_set_eigs(void* h, const double* lam);
+/* the AMG levels' Chebyshev chain of `degree` steps on one matrix (FP64),
+ * in place on x: fromZero 1 starts from x = 0 (x's input ignored) */
+void orc_cheby_chain(int n, int nf, const int* l, const int* u, const double* lo,
+                     const double* d, const double* up, int symm, double lam, double ratio,
+                     int degree, double* x, const double* b, int fromZero);
+/* start vector of the eigenvalue estimate: value of cell c (reference
+ * numbering of its level), uniform in [-1, 1) from splitmix64(c) */
+double orc_eig_start(long long c);
 
 /* Cholesky-based inverse of a dense SPD matrix (row-major), as used for the
  * coarsest level.  Returns 0 on success, -1 when not positive definite. */

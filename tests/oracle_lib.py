@@ -60,15 +60,18 @@ class Oracle:
         else:
             self.lib = ctypes.CDLL(REF_SO)
         self.prefix = prefix
-        self.lib[f"{prefix}_eigen"].restype = _c_dbl
-        self.lib[f"{prefix}_aggl_create" if prefix == "ref" else f"{prefix}_hier_create"].restype = _vp
+        # attribute access caches the function object, so restype sticks
+        # (indexing, lib["name"], returns a new object on every call)
+        getattr(self.lib, f"{prefix}_eigen").restype = _c_dbl
+        getattr(self.lib, f"{prefix}_aggl_create" if prefix == "ref"
+                else f"{prefix}_hier_create").restype = _vp
         if prefix == "ref":
             self.lib.ref_coo2ldu.restype = _vp
         else:
             self.lib.orc_amg_create.restype = _vp
 
     def _f(self, name):
-        return self.lib[f"{self.prefix}_{name}"]
+        return getattr(self.lib, f"{self.prefix}_{name}")
 
     @staticmethod
     def _mat(s):
@@ -126,6 +129,21 @@ class Oracle:
         b = _f64(b)
         self._call("cheby", s, _p(x), _p(b), _c_int(n_sweeps), _c_int(n_calls))
         return x
+
+    def cheby_chain(self, s, x, b, lam, ratio, degree, from_zero=False):
+        """The AMG levels' Chebyshev chain (FP64, new component) on one
+        matrix with a given eigenvalue estimate."""
+        x = _f64(x).copy()
+        b = _f64(b)
+        self._call("cheby_chain", s, _c_dbl(lam), _c_dbl(ratio), _c_int(degree), _p(x), _p(b),
+                   _c_int(1 if from_zero else 0))
+        return x
+
+    def eig_start(self, n):
+        f = self.lib.orc_eig_start
+        f.restype = _c_dbl
+        f.argtypes = [ctypes.c_longlong]
+        return np.array([f(c) for c in range(n)])
 
     def eigen(self, s, x, b, n_pcg=10):
         x = _f64(x).copy()
@@ -219,20 +237,24 @@ class Oracle:
 class AmgParams(ctypes.Structure):
     _fields_ = [("nCoarsest", _c_int), ("maxLevels", _c_int), ("nPre", _c_int),
                 ("nPost", _c_int), ("precision", _c_int), ("flexible", _c_int),
-                ("tol", _c_dbl), ("relTol", _c_dbl), ("maxIter", _c_int), ("minIter", _c_int)]
+                ("tol", _c_dbl), ("relTol", _c_dbl), ("maxIter", _c_int), ("minIter", _c_int),
+                ("smoother", _c_int), ("chebyDegree", _c_int), ("chebyFrom", _c_int),
+                ("eigRatio", _c_dbl)]
 
 
 class OracleAmg:
     """The C oracle's AMG-PCG (new component; no reference counterpart)."""
 
     def __init__(self, orc: Oracle, s, n_coarsest=1000, max_levels=50, n_pre=2, n_post=2,
-                 precision=0, flexible=0, tol=0.0, rel_tol=1e-10, max_iter=500, min_iter=0):
+                 precision=0, flexible=0, tol=0.0, rel_tol=1e-10, max_iter=500, min_iter=0,
+                 smoother=0, cheby_degree=3, cheby_from=0, eig_ratio=0.0):
         assert orc.prefix == "orc" and s.symm
         self.lib = orc.lib
         self.s = s
         self._keep = [_i32(s.lower_addr), _i32(s.upper_addr), _f64(s.diag), _f64(s.upper)]
         self.params = AmgParams(n_coarsest, max_levels, n_pre, n_post, precision, flexible,
-                                tol, rel_tol, max_iter, min_iter)
+                                tol, rel_tol, max_iter, min_iter, smoother, cheby_degree,
+                                cheby_from, eig_ratio)
         l, u, d, up = self._keep
         self.h = _vp(self.lib.orc_amg_create(_c_int(s.n), _c_int(s.nf), _p(l), _p(u), _p(d),
                                              _p(up), ctypes.byref(self.params)))
@@ -268,6 +290,17 @@ class OracleAmg:
                              ctypes.byref(fr), ctypes.byref(tr), ctypes.byref(cv))
         return x, dict(n_iter=it.value, init_res=ir.value, final_res=fr.value,
                        true_res=tr.value, converged=bool(cv.value))
+
+    def eigs(self):
+        """Per-level eigenvalue estimates of the Chebyshev smoother (0 where
+        a level uses Gauss-Seidel), levels 0 .. n_levels - 2."""
+        lam = np.zeros(max(self.n_levels - 1, 1))
+        self.lib.orc_amg_eigs(self.h, _p(lam))
+        return lam[:self.n_levels - 1]
+
+    def set_eigs(self, lam) -> None:
+        lam = _f64(np.resize(np.asarray(lam, dtype=np.float64), max(self.n_levels - 1, 1)))
+        self.lib.orc_amg_set_eigs(self.h, _p(lam))
 
     def set_max_iter(self, k: int) -> None:
         self.lib.orc_amg_set_max_iter(self.h, _c_int(k))

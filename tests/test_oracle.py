@@ -168,3 +168,75 @@ def test_amg_iteration_cap_can_change(orc):
     assert sf["converged"] and sf["n_iter"] > 6
     assert s1["final_res"] > s6["final_res"] > sf["final_res"]
     A.close()
+
+
+def test_cheby_chain_is_the_reference_smoother(orc, golden):
+    """The AMG levels' Chebyshev chain (a step from x, then degree - 1 more)
+    is chebySmoother::smooth after its first, estimating call: from the
+    reference's eigenvalue and the x its estimate leaves, two chains of 3
+    steps with the reference's ratio 1.5 give the reference's
+    3-sweep-x-3-call result bit for bit (golden vectors printed by the
+    reference library)."""
+    for s, g in golden:
+        x1 = g["eig_x"]
+        lam = float(g["eig"])
+        x2 = orc.cheby_chain(s, x1, s.b, lam, 1.5, 3)
+        x3 = orc.cheby_chain(s, x2, s.b, lam, 1.5, 3)
+        assert _eq(x3, g["cheby3x3"]), s.name
+
+
+def test_cheby_chain_against_reference_library(orc, ref):
+    for seed in (0, 1):
+        for s in (W.lognormal(7, 6, 5, seed=seed, permute=True),
+                  W.laplace(6, 5, 5, seed=seed, permute=True, rhs="normal")):
+            x = np.random.default_rng(seed).standard_normal(s.n)
+            for deg in (1, 2, 4):
+                lam, x1 = ref.eigen(s, x, s.b)
+                want = ref.cheby(s, x, s.b, deg, 2)
+                assert _eq(orc.cheby_chain(s, x1, s.b, lam, 1.5, deg), want), (s.name, deg)
+            # the chain from x = 0 equals the chain from a zero vector
+            z = orc.cheby_chain(s, x, s.b, 1.9, 30.0, 3, from_zero=True)
+            assert _eq(z, orc.cheby_chain(s, np.zeros(s.n), s.b, 1.9, 30.0, 3)), s.name
+
+
+def test_eig_start_vector(orc):
+    """splitmix64 start vector: deterministic, in [-1, 1), mean near 0."""
+    v = orc.eig_start(4096)
+    assert np.all(v >= -1.0) and np.all(v < 1.0)
+    assert abs(v.mean()) < 0.05 and v.std() > 0.5
+    assert len(np.unique(v)) == v.size
+
+
+def test_cheby_amg_oracle(orc):
+    """AMG-PCG with the Chebyshev V-cycle (new component): per-level
+    eigenvalue estimates of D^-1 A are within the spectrum's upper end, the
+    FP64 V-cycle is a symmetric operator, and the solve converges to the
+    true relative residual it claims, in FP64 and FP32."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    from oracle_lib import OracleAmg
+    s = W.lognormal(12, 11, 10, seed=3, permute=True)
+    for prec in (0, 1):
+        for frm in (0, 1):
+            A = OracleAmg(orc, s, n_coarsest=60, precision=prec, flexible=prec, rel_tol=1e-10,
+                          smoother=1, cheby_degree=3, cheby_from=frm, eig_ratio=30.0)
+            lam = A.eigs()
+            assert np.all(lam[:frm] == 0) and np.all(lam[frm:] > 0)
+            if frm == 0 and prec == 0:
+                M = sp.coo_matrix((np.concatenate([s.upper, s.upper, s.diag]),
+                                   (np.concatenate([s.lower_addr, s.upper_addr, np.arange(s.n)]),
+                                    np.concatenate([s.upper_addr, s.lower_addr, np.arange(s.n)]))),
+                                  shape=(s.n, s.n)).tocsr()
+                Dh = sp.diags(1.0 / np.sqrt(s.diag))
+                top = spla.eigsh(Dh @ M @ Dh, k=1, which="LA", return_eigenvectors=False)[0]
+                # Lanczos from 10 iterations approaches lambda_max from below
+                assert 0.8 * top <= lam[0] <= top * (1 + 1e-6), (lam[0], top)
+                rng = np.random.default_rng(1)
+                r1, r2 = rng.standard_normal(s.n), rng.standard_normal(s.n)
+                a, b = np.dot(A.vcycle(r1), r2), np.dot(r1, A.vcycle(r2))
+                assert abs(a - b) <= 1e-12 * abs(a), (a, b)
+            x, st = A.solve(s.b)
+            assert st["converged"], (prec, frm, st)
+            r = s.b - orc.spmv(s, x)
+            assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(s.b)
+            A.close()

@@ -85,6 +85,8 @@ SIGNATURES = {
     "unap_cuda_amg_info": (_c_int, [_c_long, _ip, _vp, _vp, _c_int, _dp,
                                     ctypes.POINTER(_c_ll)]),
     "unap_cuda_amg_vcycle": (_c_int, [_c_long, _vp, _vp]),
+    "unap_cuda_amg_eigenvalues": (_c_int, [_c_long, _vp, _c_int, _vp]),
+    "unap_cuda_set_cheby_small_rows": (_c_int, [_c_int]),
     "unap_cuda_amg_profile_vcycle": (_c_int, [_c_long, _c_int, _vp, _c_int, _ip]),
     "unap_cuda_amg_solve": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
     "unap_cuda_amg_solve_host": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
@@ -294,6 +296,12 @@ def set_packed_sweeps(mode) -> int:
     return int(load().unap_cuda_set_packed_sweeps(int(mode)))
 
 
+def set_cheby_small_rows(rows: int) -> int:
+    """Chebyshev-step launches on levels of at most `rows` rows use one-warp
+    CTAs; returns the previous threshold."""
+    return int(load().unap_cuda_set_cheby_small_rows(int(rows)))
+
+
 def set_tail_rows(tail_rows: int, single_rows: int, precision: int | None = None):
     """Thresholds of the AMG V-cycle's cluster tail kernel (0 disables it) for
     the FP64 (0) or FP32 (1) V-cycle, or both (None).  Returns the previous
@@ -363,7 +371,9 @@ def tail_cluster_size() -> int:
 class AmgParams(ctypes.Structure):
     _fields_ = [("nCoarsest", _c_int), ("maxLevels", _c_int), ("nPreSweeps", _c_int),
                 ("nPostSweeps", _c_int), ("precision", _c_int), ("flexible", _c_int),
-                ("tol", _c_dbl), ("relTol", _c_dbl), ("maxIter", _c_int), ("minIter", _c_int)]
+                ("tol", _c_dbl), ("relTol", _c_dbl), ("maxIter", _c_int), ("minIter", _c_int),
+                ("smoother", _c_int), ("chebyDegree", _c_int), ("chebyFrom", _c_int),
+                ("eigRatio", _c_dbl)]
 
 
 class DeviceAmg:
@@ -377,7 +387,9 @@ class DeviceAmg:
             kw["flexible"] = 1
         names = dict(n_coarsest="nCoarsest", max_levels="maxLevels", n_pre="nPreSweeps",
                      n_post="nPostSweeps", precision="precision", flexible="flexible",
-                     tol="tol", rel_tol="relTol", max_iter="maxIter", min_iter="minIter")
+                     tol="tol", rel_tol="relTol", max_iter="maxIter", min_iter="minIter",
+                     smoother="smoother", cheby_degree="chebyDegree", cheby_from="chebyFrom",
+                     eig_ratio="eigRatio")
         for k, v in kw.items():
             setattr(self.params, names[k], v)
         h = _c_long(0)
@@ -413,6 +425,14 @@ class DeviceAmg:
 
     def vcycle(self, r, z):
         check(load().unap_cuda_amg_vcycle(self.handle, _ptr(r), _ptr(z)))
+
+    def eigenvalues(self):
+        """Chebyshev eigenvalue estimate of every level but the coarsest
+        (0 on Gauss-Seidel levels)."""
+        lam = np.zeros(64)
+        w = _c_int()
+        check(load().unap_cuda_amg_eigenvalues(self.handle, lam.ctypes.data, 64, ctypes.byref(w)))
+        return lam[:w.value].copy()
 
     def profile_vcycle(self, reps=10):
         """Mean V-cycle ms and per-level ms (see unap_cuda_amg_profile_vcycle)."""

@@ -36,6 +36,16 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
     if (!A.host.symm) throw std::invalid_argument("AMG-PCG needs a symmetric matrix");
     if (!A.L->sweepable)
         throw std::invalid_argument("AMG smoothing needs oriented, owner-sorted faces");
+    if (params.smoother != 0 && params.smoother != 1)
+        throw std::invalid_argument("smoother must be 0 (Gauss-Seidel) or 1 (Chebyshev)");
+    if (params.smoother == 1) {
+        if (params.chebyDegree < 1 || params.chebyDegree > kChebyMaxDegree)
+            throw std::invalid_argument("Chebyshev degree must be 1 to 16");
+        if (params.chebyFrom < 0) throw std::invalid_argument("chebyFrom must be >= 0");
+        if (params.eigRatio <= 0) params.eigRatio = 1.5;  // chebySmoother.hpp:47
+        if (!(params.eigRatio > 1.0))
+            throw std::invalid_argument("Chebyshev eigenvalue ratio must be > 1");
+    }
     cudaStream_t s = A.stream;
     std::vector<double> w = mg_face_weights(A.host);
     std::vector<CoarseHost> coarse =
@@ -152,6 +162,7 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
         else
             pack_rows<double>(rows64(*lv[(size_t)k].L), lv[(size_t)k].pack, s);
     }
+    if (params.smoother == 1) setupCheby(s);
     tail_cluster_size();  // function attributes and the cluster query, outside any capture
     setupSeconds =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -178,7 +189,8 @@ size_t AmgHierarchy::deviceBytes() const
         const Lv& l = lv[k];
         if (l.own) b += l.own->deviceBytes();
         b += l.childStart.bytes() + l.child.bytes() + l.cmap.bytes() + l.x.bytes() + l.b.bytes() +
-             l.r.bytes() + l.xf.bytes() + l.bf.bytes() + l.rf.bytes() + l.pack.bytes();
+             l.r.bytes() + l.xf.bytes() + l.bf.bytes() + l.rf.bytes() + l.pack.bytes() +
+             l.t.bytes() + l.tf.bytes();
     }
     return b;
 }
@@ -213,12 +225,78 @@ float* AmgHierarchy::R<float>(int k)
 {
     return lv[(size_t)k].rf.p;
 }
+template <>
+double* AmgHierarchy::Tmp<double>(int k)
+{
+    return lv[(size_t)k].t.p;
+}
+template <>
+float* AmgHierarchy::Tmp<float>(int k)
+{
+    return lv[(size_t)k].tf.p;
+}
+
+template <class T>
+T* AmgHierarchy::chebBuf(int k, int j)
+{
+    return ((params.chebyDegree - 1 - j) % 2 == 0) ? X<T>(k) : Tmp<T>(k);
+}
+
+void AmgHierarchy::setupCheby(cudaStream_t s)
+{
+    const int L = nLevels() - 1;
+    Exec ex{s, device_max_blocks()};
+    size_t nMax = 0;
+    for (int k = 0; k < L; ++k)
+        if (isCheby(k)) nMax = std::max(nMax, (size_t)lv[(size_t)k].n);
+    if (!nMax) return;
+    DevArray<double> x(nMax), b(nMax), rD(nMax), rA(nMax), wA(nMax), pA(nMax);
+    DevArray<EigState> es(1);
+    RedPool pool;
+    pool.init(2, ex.maxBlocks, 1, s);
+    for (int k = 0; k < L; ++k) {
+        if (!isCheby(k)) continue;
+        Lv& V = lv[(size_t)k];
+        const Level& Lk = *V.L;
+        const int n = V.n;
+        // eigenDiagPCG from x = 0 on b = the splitmix64 start vector, FP64
+        k_fill<double>(ex, n, x.p, 0.0);
+        k_eig_start(ex, n, Lk.d_perm.p, b.p);
+        k_reciprocal(ex, n, Lk.d_diag.p, rD.p);
+        EigState h{};
+        h.wArA = 1.0e37;  // GREAT, eigenDiagPCG.cpp:75
+        UNAP_CK(cudaMemcpyAsync(es.p, &h, sizeof(EigState), cudaMemcpyHostToDevice, s));
+        eig_diag_pcg(ex, rows64(Lk), rD.p, x.p, b.p, rA.p, wA.p, pA.p, es.p,
+                     pool.site(0, nullptr, FIN_RES_ONLY), pool.site(1, nullptr, FIN_RES_ONLY), 10);
+        UNAP_CK(cudaMemcpyAsync(&h, es.p, sizeof(EigState), cudaMemcpyDeviceToHost, s));
+        UNAP_CK(cudaStreamSynchronize(s));
+        int nP = 0;
+        while (nP < 10 && h.alphas[nP] != 0.0) ++nP;
+        V.lam = nP >= 2 ? lanczos_max_eig(h.alphas, h.betas, nP)
+                        : (nP == 1 ? 1.0 / h.alphas[0] : 1.0);
+        cheby_coeffs(V.lam, params.eigRatio, params.chebyDegree, &V.Rth, V.d1, V.d2);
+        if (params.precision == 1)
+            V.tf.alloc((size_t)n);
+        else
+            V.t.alloc((size_t)n);
+    }
+    UNAP_CK(cudaStreamSynchronize(s));
+}
+
+std::vector<double> AmgHierarchy::eigenvalues() const
+{
+    std::vector<double> v;
+    for (int k = 0; k + 1 < nLevels(); ++k) v.push_back(lv[(size_t)k].lam);
+    return v;
+}
 
 int AmgHierarchy::tailFirst(size_t elemBytes) const
 {
     const int L = nLevels() - 1;
     const long long rows = tail_rows(params.precision);
     if (L < 1 || rows <= 0 || nc > kTailMaxCoarsest) return L;
+    // the tail kernel runs Gauss-Seidel levels only, and a tail is a suffix
+    if (params.smoother == 1 && params.chebyFrom < L) return L;
     const int C = tail_cluster_size();
     if (C < 1) return L;
     const long long single = single_rows(params.precision);
@@ -328,18 +406,54 @@ void AmgHierarchy::vcycle_level(const Exec& ex, int k, Gate g)
     }
     const Level& Lk = *lv[(size_t)k].L;
     Rows<T> Rk = rowsT<T>(Lk);
-    if (params.nPre > 0) {
+    T* r = R<T>(k);
+    const bool cheb = isCheby(k);
+    const Lv& V = lv[(size_t)k];
+    const int deg = params.chebyDegree;
+    if (cheb) {
+        // pre-smoothing from x = 0 (w shares the residual's buffer); the
+        // first step of a coarse level ran inside the restriction
+        if (k == 0) {
+            if (std::is_same<T, float>::value)
+                k_cheb_zero<T>(ex, Lk.n, Rk.diag, b, g_ext.r, chebBuf<T>(k, 0), r, (T)V.Rth, g);
+            else
+                k_cheb_zero<T>(ex, Lk.n, Rk.diag, b, nullptr, chebBuf<T>(k, 0), r, (T)V.Rth, g);
+        }
+        for (int j = 1; j < deg; ++j)
+            k_cheb_step<T>(ex, Rk, chebBuf<T>(k, j - 1), chebBuf<T>(k, j), b, r, (T)V.d1[j],
+                           (T)V.d2[j], 0, g);
+    } else if (params.nPre > 0) {
         for (int s = 0; s < params.nPre; ++s) sweep<T>(ex, k, Lk, Rk, x, b, false, s == 0, g);
     } else {
         k_fill<T>(ex, Lk.n, x, T(0));
     }
-    T* r = R<T>(k);
     k_residual<T>(ex, Rk, x, b, r, RSpec{}, g);
     const Lv& C = lv[(size_t)k + 1];
-    k_restrict<T>(ex, C.n, C.childStart.p, C.child.p, r, B<T>(k + 1), g);
+    if (isCheby(k + 1))
+        k_restrict_cheb_zero<T>(ex, C.n, C.childStart.p, C.child.p, r, B<T>(k + 1),
+                                rowsT<T>(*C.L).diag, chebBuf<T>(k + 1, 0), R<T>(k + 1),
+                                (T)C.Rth, g);
+    else
+        k_restrict<T>(ex, C.n, C.childStart.p, C.child.p, r, B<T>(k + 1), g);
     vcycle_level<T>(ex, k + 1, g);
-    k_prolong_add<T>(ex, Lk.n, C.cmap.p, X<T>(k + 1), x, g);
-    for (int s = 0; s < params.nPost; ++s) sweep<T>(ex, k, Lk, Rk, x, b, true, false, g);
+    if (cheb) {
+        // post-smoothing from x + P e: the prolongation writes the buffer the
+        // chain starts from
+        T* prev = (deg % 2 == 0) ? x : Tmp<T>(k);
+        if (prev == x)
+            k_prolong_add<T>(ex, Lk.n, C.cmap.p, X<T>(k + 1), x, g);
+        else
+            k_prolong_add_to<T>(ex, Lk.n, C.cmap.p, X<T>(k + 1), x, prev, g);
+        for (int j = 0; j < deg; ++j) {
+            T* out = chebBuf<T>(k, j);
+            k_cheb_step<T>(ex, Rk, prev, out, b, r, j == 0 ? (T)V.Rth : (T)V.d1[j],
+                           j == 0 ? T(0) : (T)V.d2[j], j == 0 ? 1 : 0, g);
+            prev = out;
+        }
+    } else {
+        k_prolong_add<T>(ex, Lk.n, C.cmap.p, X<T>(k + 1), x, g);
+        for (int s = 0; s < params.nPost; ++s) sweep<T>(ex, k, Lk, Rk, x, b, true, false, g);
+    }
     if (profOut) UNAP_CK(cudaEventRecordWithFlags((*profOut)[(size_t)k], ex.s, cudaEventRecordExternal));
 }
 
@@ -372,7 +486,35 @@ void AmgHierarchy::append_level(std::vector<Step>& out, int k, int tableBase)
     }
     const Level& Lk = *lv[(size_t)k].L;
     const bool single = mega_single_level(Lk.n);
-    if (params.nPre > 0) {
+    const bool cheb = isCheby(k);
+    const Lv& V = lv[(size_t)k];
+    const int deg = params.chebyDegree;
+    const bool fp32 = prec == 1;
+    auto chebStep = [&](const T* xin, T* xout, int j) {
+        Step s = step(ST_CHEB, single);
+        s.a = xin;
+        s.b = b;
+        s.c = xout;
+        s.d = R<T>(k);
+        s.f0 = j == 0 ? 1 : 0;
+        s.k1 = j == 0 ? V.Rth : V.d1[j];
+        s.k2 = j == 0 ? 0.0 : V.d2[j];
+        s.bytes = cheb_bytes(Lk.n, Lk.nf, fp32, j != 0);
+        out.push_back(s);
+    };
+    if (cheb) {
+        if (k == 0) {
+            Step s = step(ST_CHEB0, single);
+            s.b = b;
+            s.e = fp32 ? g_ext.r : nullptr;
+            s.c = chebBuf<T>(k, 0);
+            s.d = R<T>(k);
+            s.k1 = V.Rth;
+            s.bytes = (double)sizeof(T) * 4 * Lk.n + (fp32 ? 12.0 * Lk.n : 0.0);
+            out.push_back(s);
+        }
+        for (int j = 1; j < deg; ++j) chebStep(chebBuf<T>(k, j - 1), chebBuf<T>(k, j), j);
+    } else if (params.nPre > 0) {
         for (int sw = 0; sw < params.nPre; ++sw)
             for (int w = 0; w < Lk.nWave; ++w) {
                 Step s = step(ST_GS, single);
@@ -400,7 +542,20 @@ void AmgHierarchy::append_level(std::vector<Step>& out, int k, int tableBase)
         out.push_back(s);
     }
     const Lv& C = lv[(size_t)k + 1];
-    {
+    if (isCheby(k + 1)) {
+        Step s = step(ST_RESTRICT_CHEB0, single);
+        s.lvl = tableBase + k;  // the coarse level's rows (diagonal)
+        s.r1 = C.n;
+        s.i0 = C.childStart.p;
+        s.i1 = C.child.p;
+        s.a = R<T>(k);
+        s.c = B<T>(k + 1);
+        s.d = chebBuf<T>(k + 1, 0);
+        s.e = R<T>(k + 1);
+        s.k1 = C.Rth;
+        s.bytes = (sizeof(T) + 4.0) * Lk.n + (4.0 * sizeof(T) + 4.0) * C.n;
+        out.push_back(s);
+    } else {
         Step s = step(ST_RESTRICT, single);
         s.r1 = C.n;
         s.i0 = C.childStart.p;
@@ -411,6 +566,23 @@ void AmgHierarchy::append_level(std::vector<Step>& out, int k, int tableBase)
         out.push_back(s);
     }
     append_level<T>(out, k + 1, tableBase);
+    if (cheb) {
+        T* prev = (deg % 2 == 0) ? x : Tmp<T>(k);
+        Step s = step(prev == x ? ST_PROLONG_ADD : ST_PROLONG_TO, single);
+        s.r1 = Lk.n;
+        s.i0 = C.cmap.p;
+        s.a = X<T>(k + 1);
+        s.b = x;
+        s.c = prev;
+        s.bytes = (2.0 * sizeof(T) + 4.0) * Lk.n + (double)sizeof(T) * C.n;
+        out.push_back(s);
+        for (int j = 0; j < deg; ++j) {
+            T* o = chebBuf<T>(k, j);
+            chebStep(prev, o, j);
+            prev = o;
+        }
+        return;
+    }
     {
         Step s = step(ST_PROLONG_ADD, single);
         s.r1 = Lk.n;
@@ -454,7 +626,8 @@ void AmgHierarchy::appendVcycle(std::vector<Step>& out, std::vector<LevelRows>& 
         s.a = r;
         s.c = lv[0].bf.p;
         s.bytes = 12.0 * n0;
-        out.push_back(s);
+        // a Chebyshev finest level converts r inside its first step
+        if (!isCheby(0)) out.push_back(s);
         append_level<float>(out, 0, tableBase);
         Step t;
         t.op = ST_F2D;
@@ -475,7 +648,8 @@ void AmgHierarchy::vcycle(const Exec& ex, const double* r, double* z, Gate g)
     g_ext.z = z;
     curTail = tailFirst(params.precision == 1 ? sizeof(float) : sizeof(double));
     if (params.precision == 1) {
-        k_d2f(ex, lv[0].n, r, lv[0].bf.p);
+        // a Chebyshev finest level converts r inside its first step
+        if (!isCheby(0)) k_d2f(ex, lv[0].n, r, lv[0].bf.p);
         vcycle_level<float>(ex, 0, g);
         k_f2d(ex, lv[0].n, lv[0].xf.p, z);
     } else {

@@ -4,6 +4,7 @@
 #include <memory>
 #include <vector>
 
+#include "cheby.hpp"
 #include "engine.hpp"
 #include "tail.hpp"
 
@@ -36,6 +37,10 @@ struct AmgParams {
     int maxLevels = 50;
     int nPre = 2, nPost = 2;
     int precision = 0;  // 0 FP64 V-cycle, 1 FP32 V-cycle (coarsest solve FP64)
+    int smoother = 0;     // 0 Gauss-Seidel, 1 Chebyshev on levels >= chebyFrom
+    int chebyDegree = 3;  // Chebyshev steps before and after the coarse correction
+    int chebyFrom = 0;    // first Chebyshev level (Gauss-Seidel above it)
+    double eigRatio = 30; // interval [lam / eigRatio, 1.1 lam]; <= 0: the reference's 1.5
 };
 
 // Device hierarchy for AMG as a fixed, symmetric PCG preconditioner:
@@ -43,6 +48,14 @@ struct AmgParams {
 //                e = V(k+1, b'); x += P e; nPost backward GS sweeps
 //   level L:     x = Minv b (dense FP64 inverse, rows summed in column order)
 // R sums the aggregate's cells in ascending cell order, P injects.
+// With the Chebyshev smoother a level k >= chebyFrom replaces the sweeps by
+// chebyDegree Chebyshev steps from x = 0 before, and from x after, the
+// coarse correction (cheby.hpp), over [lam_k / eigRatio, 1.1 lam_k] with
+// lam_k the reference's diagonal-PCG estimate of the level's largest
+// eigenvalue of D^-1 A taken once at setup (FP64, from x = 0 and the
+// splitmix64 start vector); the same polynomial on both sides keeps the
+// preconditioner symmetric.  A level's first step from x = 0 is fused into
+// the restriction that produces its right-hand side.
 class AmgHierarchy {
 public:
     AmgHierarchy(Matrix& A, const AmgParams& p);
@@ -71,7 +84,11 @@ public:
         DevArray<int> cmap;               // prolongation from this level (k >= 1)
         DevArray<double> x, b, r;
         DevArray<float> xf, bf, rf;
+        DevArray<double> t;  // second Chebyshev iterate (FP64 V-cycle)
+        DevArray<float> tf;  // second Chebyshev iterate (FP32 V-cycle)
         PackedRows pack;  // row-packed copy for the cluster tail (coarse levels)
+        double lam = 0;   // Chebyshev: eigenvalue estimate and coefficients
+        double Rth = 0, d1[kChebyMaxDegree] = {}, d2[kChebyMaxDegree] = {};
     };
     std::vector<Lv> lv;
     DevArray<double> Minv;  // coarsest dense inverse, column-major
@@ -83,8 +100,21 @@ public:
     // the current thresholds and shared-memory capacity for elements of
     // elemBytes bytes (nLevels() - 1: no tail)
     int tailFirst(size_t elemBytes) const;
+    // level k (< the coarsest) is smoothed by Chebyshev steps
+    bool isCheby(int k) const
+    {
+        return params.smoother == 1 && k >= params.chebyFrom && k < nLevels() - 1;
+    }
+    std::vector<double> eigenvalues() const;
 
 private:
+    void setupCheby(cudaStream_t s);
+    template <class T>
+    T* Tmp(int k);
+    // the buffer holding step j of a level's pre- (or post-) smoothing chain,
+    // chosen so that the last step lands in X(k)
+    template <class T>
+    T* chebBuf(int k, int j);
     Matrix& A;
     template <class T>
     void vcycle_level(const Exec& ex, int k, Gate g);

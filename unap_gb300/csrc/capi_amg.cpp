@@ -82,6 +82,10 @@ void unap_cuda_amg_default_params(unap_cuda_amg_params* p)
     p->relTol = 1e-10;
     p->maxIter = 500;
     p->minIter = 0;
+    p->smoother = 0;
+    p->chebyDegree = 3;
+    p->chebyFrom = 0;
+    p->eigRatio = 30.0;
 }
 
 int unap_cuda_amg_create(long int* amg, long int matrix, const unap_cuda_amg_params* p)
@@ -102,6 +106,10 @@ int unap_cuda_amg_create(long int* amg, long int matrix, const unap_cuda_amg_par
         ap.nPre = h->p.nPreSweeps;
         ap.nPost = h->p.nPostSweeps;
         ap.precision = h->p.precision;
+        ap.smoother = h->p.smoother;
+        ap.chebyDegree = h->p.chebyDegree;
+        ap.chebyFrom = h->p.chebyFrom;
+        ap.eigRatio = h->p.eigRatio;
         h->H = std::make_unique<AmgHierarchy>(*h->A, ap);
         h->P = std::make_unique<AmgPrecond>(*h->H);
         h->K = std::make_unique<Krylov>(*h->A, h->P.get(), Method::PCG);
@@ -172,6 +180,18 @@ int unap_cuda_amg_profile_vcycle(long int amg, int reps, double* ms, int maxOut,
     });
 }
 
+int unap_cuda_amg_eigenvalues(long int amg, double* lam, int maxOut, int* written)
+{
+    return guarded([&] {
+        AmgHandle* h = amg_from(amg);
+        std::vector<double> v = h->H->eigenvalues();
+        int w = 0;
+        for (; w < (int)v.size() && w < maxOut; ++w)
+            if (lam) lam[w] = v[(size_t)w];
+        if (written) *written = w;
+    });
+}
+
 int unap_cuda_amg_solve(long int amg, double* x, const double* b, unap_cuda_stats* stats)
 {
     return guarded([&] {
@@ -211,6 +231,8 @@ int unap_cuda_set_wave_pdl(int on) { return set_wave_pdl(on); }
 int unap_cuda_set_wave_grid(int oneRowPerThread) { return set_wave_grid(oneRowPerThread); }
 
 int unap_cuda_set_packed_sweeps(int mode) { return set_packed_sweeps(mode); }
+
+int unap_cuda_set_cheby_small_rows(int rows) { return set_cheby_small_rows(rows); }
 
 int unap_cuda_set_tail_rows(int precision, long long tailRows, long long singleRows,
                             long long* oldTailRows, long long* oldSingleRows)

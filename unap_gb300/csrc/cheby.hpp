@@ -1,0 +1,80 @@
+// Chebyshev smoothing (chebySmoother.cpp:44-148) and its largest-eigenvalue
+// estimate (eigenDiagPCG.cpp:11-361) on the device, shared by the
+// reference MGSolver (mg.cu) and the AMG V-cycle (amg.cu).
+//
+// A Chebyshev step is SpMV-shaped: every row reads the previous iterate of
+// its neighbours and nothing else of the step, so a level is one launch per
+// step (no wavefronts), with the iterate double-buffered.  Per row, in the
+// reference's arithmetic order (A x as lduMatrix::spMV sums it, rD = 1/diag):
+//   first step from x = 0:  w = rD b Rtheta;              x = w
+//   first step from x:      w = rD (b - A x) Rtheta;      x = x + w
+//   step j >= 1:            w = d1_j w + d2_j rD (b - A x); x = x + w
+#pragma once
+
+#include "kernels.hpp"
+
+namespace unapgpu {
+
+constexpr int kChebyMaxDegree = 16;
+
+// Eigenvalue estimate state of one smoother (eigenDiagPCG.cpp:48-238:
+// diagonal-PCG iterations recording alpha and beta).
+struct EigState {
+    double wArA, wArAold, wApA, alpha, beta;
+    int broken, pad;
+    double alphas[16], betas[16];
+    double maxEig;
+};
+
+// eigenDiagPCG::diagPCGLoops: nIt (<= 16) diagonal-PCG iterations on
+// (x, b), x updated in place.  es must hold wArA = GREAT and zeros on entry;
+// a breakdown (|wArA| < VSMALL) sets es->broken and leaves the remaining
+// alphas 0.  rA, wA, pA: n-vector scratch; wr and al: two reduction sites.
+void eig_diag_pcg(const Exec& ex, const Rows<double>& A, const double* rD, double* x,
+                  const double* b, double* rA, double* wA, double* pA, EigState* es,
+                  const RSpec& wr, const RSpec& al, int nIt);
+
+// eigenDiagPCG::computeMaxEig (eigenDiagPCG.cpp:242-361) on the host: the
+// Lanczos tridiagonal of nP >= 2 iterations, Sturm-sequence bisection to a
+// band of 1e-5.
+double lanczos_max_eig(const double* alphas, const double* betas, int nP);
+
+// Start vector of the AMG levels' eigenvalue estimate: cell c (reference
+// numbering of its level) gets a uniform value in [-1, 1) from splitmix64.
+void k_eig_start(const Exec& ex, int n, const int* perm, double* b);
+
+// r[i] = 1 / d[i] (lduDiagPrecond.cpp:13-41)
+void k_reciprocal(const Exec& ex, int n, const double* d, double* r);
+
+// chebySmoother.cpp:62-108 for the interval [lam / ratio, 1.1 lam]:
+// Rtheta of the first step and (d1[j], d2[j]) of steps j = 1 .. deg - 1.
+void cheby_coeffs(double lam, double ratio, int deg, double* Rtheta, double* d1, double* d2);
+
+// One Chebyshev step on every row of A: first != 0 is the first step from a
+// nonzero x (c1 = Rtheta), else a later step (c1 = d1, c2 = d2).  xin and
+// xout are distinct.  Launched with programmatic dependent launch when
+// wave_pdl() is on: the kernel loads its rows' matrix data and b before it
+// waits for the previous kernel.
+template <class T>
+void k_cheb_step(const Exec& ex, const Rows<T>& A, const T* xin, T* xout, const T* b, T* w, T c1,
+                 T c2, int first, Gate g);
+// First step from x = 0: w = x = rD b Rtheta.  With r64 != null (FP32
+// levels entered from FP64) b is first set to (float)r64.
+template <class T>
+void k_cheb_zero(const Exec& ex, int n, const T* diag, T* b, const double* r64, T* x, T* w, T Rth,
+                 Gate g);
+// Restriction into a Chebyshev level fused with that level's first step:
+// coarse[C] = sum of the children (ascending), then w = x = rD coarse Rtheta.
+template <class T>
+void k_restrict_cheb_zero(const Exec& ex, int nC, const int* childStart, const int* child,
+                          const T* fine, T* coarse, const T* diagC, T* xC, T* wC, T Rth, Gate g);
+// Out-of-place prolongation: xout[i] = xin[i] + coarse[cmap[i]].
+template <class T>
+void k_prolong_add_to(const Exec& ex, int n, const int* cmap, const T* coarse, const T* xin,
+                      T* xout, Gate g);
+
+// Rows per level below which Chebyshev-step launches use one-warp CTAs
+// (spread over more SMs); returns the previous value.
+int set_cheby_small_rows(int rows);
+
+}  // namespace unapgpu

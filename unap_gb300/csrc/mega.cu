@@ -201,6 +201,82 @@ __device__ void exec_dic_bwd(const Step& s, const LevelRows& L, const MegaArgs& 
     put_partial<1>(v, g, s.red, s.f0 != 0, single);
 }
 
+template <class T>
+__device__ void exec_cheb(const Step& s, const LevelRows& L, int first, int stride)
+{
+    const Rows<T>& A = rows_of<T>(L);
+    const T* xin = (const T*)s.a;
+    const T* b = (const T*)s.b;
+    T* xout = (T*)s.c;
+    T* w = (T*)s.d;
+    const T c1 = (T)s.k1, c2 = (T)s.k2;
+    for (int r = first; r < A.n; r += stride) {
+        const T acc = row_apply<T, XL_CG>(A, r, xin);
+        const T rD = T(1) / ldg(A.diag + r);
+        const T bb = __ldcg(b + r);
+        T wi;
+        if (s.f0)
+            wi = rD * (bb - acc) * c1;
+        else
+            wi = c1 * __ldcg(w + r) + c2 * rD * (bb - acc);
+        w[r] = wi;
+        xout[r] = __ldcg(xin + r) + wi;
+    }
+}
+
+template <class T>
+__device__ void exec_cheb0(const Step& s, const LevelRows& L, int first, int stride)
+{
+    const Rows<T>& A = rows_of<T>(L);
+    T* b = (T*)s.b;
+    const double* r64 = (const double*)s.e;
+    T* x = (T*)s.c;
+    T* w = (T*)s.d;
+    const T Rth = (T)s.k1;
+    for (int i = first; i < A.n; i += stride) {
+        T bi;
+        if (r64) {
+            bi = (T)__ldcg(r64 + i);
+            b[i] = bi;
+        } else {
+            bi = __ldcg(b + i);
+        }
+        const T rD = T(1) / ldg(A.diag + i);
+        const T wi = rD * bi * Rth;
+        w[i] = wi;
+        x[i] = wi;
+    }
+}
+
+template <class T>
+__device__ void exec_restrict_cheb0(const Step& s, const LevelRows& L, int first, int stride)
+{
+    const Rows<T>& A = rows_of<T>(L);
+    const T* fine = (const T*)s.a;
+    T* coarse = (T*)s.c;
+    T* x = (T*)s.d;
+    T* w = (T*)s.e;
+    const T Rth = (T)s.k1;
+    for (int c = first; c < s.r1; c += stride) {
+        T acc = T(0);
+        for (int k = s.i0[c]; k < s.i0[c + 1]; ++k) acc += __ldcg(fine + s.i1[k]);
+        coarse[c] = acc;
+        const T rD = T(1) / ldg(A.diag + c);
+        const T wi = rD * acc * Rth;
+        w[c] = wi;
+        x[c] = wi;
+    }
+}
+
+template <class T>
+__device__ void exec_prolong_to(const Step& s, int first, int stride)
+{
+    const T* coarse = (const T*)s.a;
+    const T* xin = (const T*)s.b;
+    T* xout = (T*)s.c;
+    for (int i = first; i < s.r1; i += stride) xout[i] = __ldcg(xin + i) + __ldcg(coarse + s.i0[i]);
+}
+
 __device__ void exec_step(const Step& s, const MegaArgs& g, bool single)
 {
     const int first = single ? threadIdx.x : blockIdx.x * blockDim.x + threadIdx.x;
@@ -256,6 +332,30 @@ __device__ void exec_step(const Step& s, const MegaArgs& g, bool single)
     case ST_SLEEP:
         if (blockIdx.x == 0 && threadIdx.x == 0)
             for (int us = 0; us < s.f0 && us < 1000000; ++us) __nanosleep(1000);
+        break;
+    case ST_CHEB:
+        if (s.prec)
+            exec_cheb<float>(s, L, first, stride);
+        else
+            exec_cheb<double>(s, L, first, stride);
+        break;
+    case ST_CHEB0:
+        if (s.prec)
+            exec_cheb0<float>(s, L, first, stride);
+        else
+            exec_cheb0<double>(s, L, first, stride);
+        break;
+    case ST_RESTRICT_CHEB0:
+        if (s.prec)
+            exec_restrict_cheb0<float>(s, L, first, stride);
+        else
+            exec_restrict_cheb0<double>(s, L, first, stride);
+        break;
+    case ST_PROLONG_TO:
+        if (s.prec)
+            exec_prolong_to<float>(s, first, stride);
+        else
+            exec_prolong_to<double>(s, first, stride);
         break;
     case ST_DIC_FWD: exec_dic_fwd(s, L, first, stride); break;
     case ST_DIC_BWD: exec_dic_bwd(s, L, g, first, stride, single); break;

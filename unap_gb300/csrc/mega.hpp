@@ -39,6 +39,13 @@ enum StepOp : int {
     ST_RESID_NORM,    // r = b - A x; partial red += r.r (FP64, lvl)
     ST_COPY,          // c = a (double)
     ST_SLEEP,         // CTA 0 thread 0 sleeps f0 microseconds (bounded; barrier self-test)
+    ST_CHEB,          // Chebyshev step on level lvl (cheby.hpp): a = x in, c = x out,
+                      // b = b, d = w; f0 = first step from x; k1, k2 coefficients
+    ST_CHEB0,         // first Chebyshev step from x = 0: c = x, d = w, b = b (first set
+                      // to (float) e when e != null); k1 = Rtheta; diag of level lvl
+    ST_RESTRICT_CHEB0,// ST_RESTRICT fused with the coarse level's ST_CHEB0: d = x,
+                      // e = w of the coarse level lvl; k1 = its Rtheta
+    ST_PROLONG_TO,    // c[i] = b[i] + a[i0[i]] (out-of-place prolongation)
 };
 
 struct Step {
@@ -56,6 +63,7 @@ struct Step {
     const void* e = nullptr;
     const int* i0 = nullptr;
     const int* i1 = nullptr;
+    double k1 = 0, k2 = 0;  // Chebyshev coefficients
     double bytes = 0;  // algorithmic DRAM bytes of the step (host bookkeeping)
 };
 
@@ -68,6 +76,15 @@ inline double sweep_bytes(int rows, int n, int nf, bool fp32)
 {
     const double cb = fp32 ? 16.0 : 32.0, fb = fp32 ? 12.0 : 16.0;
     return rows * cb + (n > 0 ? (double)rows / n * nf * fb : 0.0);
+}
+
+// Algorithmic bytes of a Chebyshev step over a level: per cell diag, b, x
+// gathered once, x write, w write and (after the first step) w read; per
+// face one value and two int32 addresses.
+inline double cheb_bytes(int n, int nf, bool fp32, bool readW)
+{
+    const double e = fp32 ? 4.0 : 8.0;
+    return n * e * (readW ? 6.0 : 5.0) + (double)nf * (fp32 ? 12.0 : 16.0);
 }
 
 struct LevelRows {

@@ -63,73 +63,8 @@ __global__ void __launch_bounds__(kBlock) scaling_kernel(int n, const double* __
     reduce_launch<2>(v, red, [&](const double (&t)[2]) { *sfOut = t[0] / (t[1] + SMALL_D); });
 }
 
-// ---- eigenDiagPCG (eigenDiagPCG.cpp:48-238, 242-361) ---------------------
-__global__ void __launch_bounds__(kBlock) eig_wr_kernel(int n, const double* __restrict__ rD,
-                                                        const double* __restrict__ rA,
-                                                        double* __restrict__ wA, EigState* es,
-                                                        int it, RSpec red)
-{
-    if (es->broken) return;
-    double v[1] = {0.0};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double w = rD[i] * rA[i];
-        wA[i] = w;
-        v[0] += w * rA[i];
-    }
-    reduce_launch<1>(v, red, [&](const double (&t)[1]) {
-        es->wArAold = es->wArA;
-        es->wArA = t[0];
-        if (fabs(es->wArA) < VSMALL_D) {
-            es->broken = 1;
-        } else if (it == 0) {
-            es->betas[0] = 0.0;
-        } else {
-            es->beta = es->wArA / es->wArAold;
-            es->betas[it] = es->beta;
-        }
-    });
-}
-
-__global__ void eig_p_kernel(int n, const double* __restrict__ wA, double* __restrict__ pA,
-                             const EigState* es, int it)
-{
-    if (es->broken) return;
-    const double beta = es->beta;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        pA[i] = it == 0 ? wA[i] : wA[i] + beta * pA[i];
-}
-
-__global__ void __launch_bounds__(kBlock) eig_alpha_kernel(Rows<double> A,
-                                                           const double* __restrict__ pA,
-                                                           double* __restrict__ wA, EigState* es,
-                                                           int it, RSpec red)
-{
-    if (es->broken) return;
-    double v[1] = {0.0};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
-        double w = row_apply<double>(A, i, pA);
-        wA[i] = w;
-        v[0] += w * pA[i];
-    }
-    reduce_launch<1>(v, red, [&](const double (&t)[1]) {
-        es->wApA = t[0];
-        es->alpha = es->wArA / es->wApA;
-        es->alphas[it] = es->alpha;
-    });
-}
-
-__global__ void eig_update_kernel(int n, double* __restrict__ x, double* __restrict__ rA,
-                                  const double* __restrict__ pA, const double* __restrict__ wA,
-                                  const EigState* es)
-{
-    if (es->broken) return;
-    const double alpha = es->alpha;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        x[i] += alpha * pA[i];
-        rA[i] -= alpha * wA[i];
-    }
-}
-
+// ---- eigenDiagPCG (eigenDiagPCG.cpp:242-361); the diagonal-PCG loops are
+// eig_diag_pcg (cheby.cu) --------------------------------------------------
 // Lanczos tridiagonal + Sturm-sequence bisection to 1e-5 (k = 1)
 __global__ void eig_sturm_kernel(EigState* es, int nP)
 {
@@ -365,22 +300,10 @@ void MgSolver::eigen_estimate(int slot, int k, double* xk, const double* bk)
     EigState* es = eig.p + slot;
     UNAP_CK(cudaMemcpyAsync(es, &h, sizeof(EigState), cudaMemcpyHostToDevice, ex.s));
     Rows<double> R = rows64(*K.L);
-    k_residual<double>(ex, R, xk, bk, K.acf.p, RSpec{}, Gate{});  // rA = b - A x
-    double* rA = K.acf.p;
-    double* wA = K.w.p;
-    double* pA = K.p.p;
-    for (int it = 0; it < 10; ++it) {
-        tick();
-        eig_wr_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, K.rD.p, rA, wA, es, it,
-                                                      pool.site(M_EIGWR, nullptr, FIN_RES_ONLY));
-        tick();
-        eig_p_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, wA, pA, es, it);
-        tick();
-        eig_alpha_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(R, pA, wA, es, it,
-                                                         pool.site(M_EIGA, nullptr, FIN_RES_ONLY));
-        tick();
-        eig_update_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, xk, rA, pA, wA, es);
-    }
+    (void)n;
+    eig_diag_pcg(ex, R, K.rD.p, xk, bk, K.acf.p, K.w.p, K.p.p, es,
+                 pool.site(M_EIGWR, nullptr, FIN_RES_ONLY), pool.site(M_EIGA, nullptr, FIN_RES_ONLY),
+                 10);
     tick();
     eig_sturm_kernel<<<1, 1, 0, ex.s>>>(es, 10);
 }

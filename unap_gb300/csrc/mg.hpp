@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "amg.hpp"
+#include "cheby.hpp"
 #include "small_solve.hpp"
 
 namespace unapgpu {
@@ -17,15 +18,6 @@ struct MgParams {
     int scaleCorr = -1;   // -1: A.symm() (MG.cpp:13)
     double tol = 0.0, relTol = 1e-6;
     int maxIter = 1000, minIter = 0;
-};
-
-// Eigenvalue estimate state of one Chebyshev smoother slot
-// (eigenDiagPCG.cpp:48-238, 10 diagonal-PCG iterations).
-struct EigState {
-    double wArA, wArAold, wApA, alpha, beta;
-    int broken, pad;
-    double alphas[16], betas[16];
-    double maxEig;
 };
 
 // MGSolver::solve (MGSolve.cpp:17-187) with Vcycle (Vcycle.cpp:27-332),
