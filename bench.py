@@ -3,24 +3,31 @@
 Workload (default ``c4``): 256^3 variable-coefficient Poisson with log-normal
 cell conductances exp(N(0, 2^2)), harmonic-mean face coefficients, a seeded
 random cell permutation (unstructured LDU addressing), rhs N(0,1) with zero
-mean, diagonal shift 1e-8.  The timed method is the mixed-precision AMG-PCG
-(FP32 V-cycle with forward/backward Gauss-Seidel 2/2 inside an FP64 flexible
-PCG, dense FP64 coarsest solve, coarsest <= 1000 cells); the plain FP64
-AMG-PCG on the same matrix is timed beside it.
+mean, diagonal shift 1e-8.  The timed method is the mixed-precision AMG-PCG:
+an FP32 V-cycle inside an FP64 flexible PCG, dense FP64 coarsest solve,
+coarsest <= 1000 cells, the finest level smoothed by forward/backward
+Gauss-Seidel 2/2 and every coarser level by the reference's Chebyshev
+iteration of degree 3 (eigenvalue interval [lambda/30, 1.1 lambda], lambda
+estimated once per level at setup).  The same method in FP64 is timed beside
+it, and the all-Gauss-Seidel V-cycle in both precisions for comparison.
 
 A "step" is one complete solve from x = 0 to ||b - A x|| <= 1e-10 ||b||
-(setup -- agglomeration, coarse matrices, coarsest inverse -- is done once,
-outside the timed region, as for the reference's handle API).  `value` is
-the device time of one solve (CUDA events on the solver's stream), inputs
-resident in HBM; `e2e` is the same solve through the host-array C ABI entry
-point (unap_cuda_amg_solve_host) with the b/x host<->device copies inside.
+(setup -- agglomeration, coarse matrices, eigenvalue estimates, coarsest
+inverse -- is done once, outside the timed region, as for the reference's
+handle API).  `value` is the device time of one solve (CUDA events on the
+solver's stream), inputs resident in HBM; `e2e` is the same solve through
+the host-array C ABI entry point (unap_cuda_amg_solve_host) with the b/x
+host<->device copies inside.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c4]
     python bench.py --impl reference      # the CPU reference arm
 
-A 1-GPU run also serves the seeded 200-request stream of config c5
-(`serving`: solves/s and p50/p99 latency beside the one-at-a-time FP64
-path; `--serve 0` skips it).
+A 1-GPU run also reports configs c1-c3 (GPU device time, e2e through the
+reference's one-shot C ABI calls, the oracle's CPU time on a bounded sample)
+and serves the seeded 2000-request stream of config c5 (`serving`: solves/s
+and p50/p99 latency from each request's scheduled arrival, beside the plain
+one-at-a-time FP64 path queued on the same arrival schedule; `--serve 0`
+skips it, `--no-configs` skips c1-c3).
 
 Multi-GPU runs are independent replicas (one system per rank, no collective
 on the data path); the reported time is the max over ranks.
@@ -41,16 +48,27 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
+# the headline V-cycle: Gauss-Seidel on the finest level, Chebyshev of
+# degree 3 below it
+CHEBY = dict(smoother=1, cheby_degree=3, cheby_from=1, eig_ratio=30.0)
 WORKLOADS = {
-    "c4": dict(desc="256^3 log-normal(sigma=2) Poisson, permuted LDU, mixed AMG-PCG tol 1e-10",
-               method="amg", precision=1),
-    "c2": dict(desc="128^3 7-point Laplacian, permuted LDU, FP64 AMG-PCG tol 1e-10",
-               method="amg", precision=0),
+    "c4": dict(desc="256^3 log-normal(sigma=2) Poisson, permuted LDU, mixed AMG-PCG "
+                    "(finest level Gauss-Seidel 2/2, Chebyshev degree 3 below), tol 1e-10",
+               method="amg", precision=1, amg=CHEBY, rel_tol=1e-10),
+    "c2": dict(desc="128^3 7-point Laplacian, permuted LDU, FP64 AMG-PCG "
+                    "(symmetric Gauss-Seidel 2/2), tol 1e-10",
+               method="amg", precision=0, amg=dict(smoother=0), rel_tol=1e-10),
+}
+# configs reported beside the headline (reference methods where it has them)
+CONFIGS = {
+    "c1": dict(desc="32^3 Laplacian, natural order, PCG+DIC, tol 1e-8", kind="krylov",
+               method=0, precond=2, rel_tol=1e-8),
+    "c2": dict(desc="128^3 permuted Laplacian, FP64 AMG-PCG (Gauss-Seidel 2/2), tol 1e-10",
+               kind="amg", precision=0, amg=dict(smoother=0), rel_tol=1e-10),
+    "c3": dict(desc="200^3 permuted convection-diffusion (Pe 5), PBiCGStab+DILU, tol 1e-9",
+               kind="krylov", method=1, precond=3, rel_tol=1e-9),
 }
 L2_BYTES = 129 * 2 ** 20
-# DRAM bytes / algorithmic bytes of a whole FP32 Gauss-Seidel sweep, measured
-# in situ (no cache flush) with ncu on the 192^3 log-normal matrix
-SWEEP_TRAFFIC_RATIO = 1.29
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -147,85 +165,121 @@ def barrier(dist, device=None):
             dist.barrier()
 
 
-def gs32_sweep_bytes(n: int, nf: int) -> int:
-    """Algorithmic bytes of one FP32 Gauss-Seidel sweep over a symmetric LDU
-    matrix: per cell b, x read, x write, diag (4 B each); per face one value
-    and two int32 addresses (compulsory LDU data, each touched once)."""
-    return 16 * n + 12 * nf
+def spmv64_bytes(n: int, nf: int, symm: bool = True) -> int:
+    """Algorithmic bytes of an FP64 LDU SpMV: diag, x, y (8 B each) per cell;
+    per face one value (two if asymmetric) and two int32 addresses."""
+    return 24 * n + (16 if symm else 24) * nf
 
 
-def spmv64_bytes(n: int, nf: int) -> int:
-    """Algorithmic bytes of an FP64 symmetric LDU SpMV: diag, x, y (8 B each)
-    per cell, one value and two int32 addresses per face."""
-    return 24 * n + 16 * nf
+def amg_kwargs(cfg) -> dict:
+    """DeviceAmg / OracleAmg keyword arguments of a workload's V-cycle."""
+    return dict(cfg.get("amg", {}))
 
 
-def cpu_baseline(s, gpu_iters: int, budget_s: float = 25.0):
-    """The oracle's FP64 AMG-PCG (C restatement, one host thread) on the same
-    matrix: setup untimed, then a bounded sample of PCG iterations timed and
-    scaled to the iteration count the GPU's FP64 solve needed."""
+def oracle_amg_sample(s, cfg, gpu_iters: int, caps=(1, 2)):
+    """The oracle's FP64 AMG-PCG (C restatement, one host thread) on `s` with
+    the workload's V-cycle: hierarchy and eigenvalue estimates untimed, then
+    solves capped at caps[0] and caps[1] iterations; the time per iteration
+    is their difference over the iterations between, the fixed cost (initial
+    residual, allocations, final true residual) what is left of the shorter
+    one, and the estimate is fixed + per_iter * gpu_iters."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import Oracle, OracleAmg
     orc = Oracle("orc")
     t0 = time.perf_counter()
-    probe = OracleAmg(orc, s, n_coarsest=1000, precision=0, rel_tol=1e-10, max_iter=1)
+    O = OracleAmg(orc, s, n_coarsest=1000, precision=0, rel_tol=cfg["rel_tol"],
+                  max_iter=caps[0], **amg_kwargs(cfg))
     setup = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    probe.solve(s.b)
-    t1 = time.perf_counter() - t0
-    probe.close()
-    k = max(2, min(20, int(budget_s / max(t1, 1e-3))))
-    O = OracleAmg(orc, s, n_coarsest=1000, precision=0, rel_tol=1e-10, max_iter=k)
-    t0 = time.perf_counter()
-    _, st = O.solve(s.b)
-    tk = time.perf_counter() - t0
+    t = []
+    for k in caps:
+        O.set_max_iter(k)
+        t0 = time.perf_counter()
+        O.solve(s.b)
+        t.append(time.perf_counter() - t0)
     O.close()
-    per_iter = (tk - t1) / max(k - 1, 1)
-    est = t1 + per_iter * max(gpu_iters - 1, 0)
-    return {"value": est, "unit": "s", "cores": 1, "kind": "port",
-            "sample": (f"oracle FP64 AMG-PCG on the same {s.n}-cell matrix: {k} PCG iterations "
-                       f"timed ({tk:.2f} s, {per_iter:.3f} s/iteration after the first), scaled "
-                       f"to the GPU FP64 solve's {gpu_iters} iterations; setup {setup:.1f} s "
-                       f"untimed"),
-            "iterations_timed": st["n_iter"]}
+    per_iter = max((t[1] - t[0]) / (caps[1] - caps[0]), 1e-9)
+    fixed = max(t[0] - caps[0] * per_iter, 0.0)
+    return {"value": fixed + per_iter * gpu_iters, "unit": "s", "cores": 1, "kind": "port",
+            "per_iteration_s": per_iter, "fixed_s": fixed, "setup_s": setup,
+            "sample": (f"oracle FP64 AMG-PCG (same V-cycle) on the same {s.n}-cell matrix: solves "
+                       f"capped at {caps[0]} and {caps[1]} iterations timed ({t[0]:.2f} s, "
+                       f"{t[1]:.2f} s), {per_iter:.3f} s/iteration + {fixed:.2f} s fixed cost, "
+                       f"scaled to the GPU FP64 solve's {gpu_iters} iterations; setup "
+                       f"{setup:.1f} s untimed")}
+
+
+def oracle_krylov_sample(s, cfg, gpu_iters: int, full_below: int = 200_000):
+    """The oracle's PCG / PBiCGStab (the reference's methods restated, one
+    host thread): a full solve on small systems, else solves capped at 1 and
+    3 iterations scaled to the GPU's iteration count (fixed cost separate)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import Oracle
+    orc = Oracle("orc")
+    fn = orc.pcg if cfg["method"] == 0 else orc.pbicgstab
+    if s.n <= full_below:
+        t0 = time.perf_counter()
+        _, st = fn(s, cfg["precond"], s.b, rel_tol=cfg["rel_tol"], max_iter=5000)
+        dt = time.perf_counter() - t0
+        return {"value": dt, "unit": "s", "cores": 1, "kind": "port", "iterations": st["n_iter"],
+                "sample": f"oracle full solve, {st['n_iter']} iterations"}
+    t = []
+    for k in (1, 3):
+        t0 = time.perf_counter()
+        fn(s, cfg["precond"], s.b, rel_tol=cfg["rel_tol"], max_iter=k)
+        t.append(time.perf_counter() - t0)
+    per_iter = max((t[1] - t[0]) / 2, 1e-9)
+    fixed = max(t[0] - per_iter, 0.0)
+    return {"value": fixed + per_iter * gpu_iters, "unit": "s", "cores": 1, "kind": "port",
+            "per_iteration_s": per_iter, "fixed_s": fixed,
+            "sample": (f"oracle solves capped at 1 and 3 iterations ({t[0]:.2f} s, {t[1]:.2f} s), "
+                       f"scaled to the GPU solve's {gpu_iters} iterations")}
 
 
 def reference_arm(args, rank, dist):
     """CPU reference arm: the oracle (the reference restated; the reference's
-    own build needs its source tree, absent on the GPU host) on the host."""
+    own build needs its source tree, absent on the GPU host) on the host.
+    The reference has no AMG-PCG (its MGPrecond is a stub), so this is the
+    restatement's FP64 AMG-PCG with the workload's V-cycle."""
     if rank != 0:
         return
     from unap_gb300 import workloads as W
     wl = WORKLOADS[args.workload]
     s = W.config(args.workload, args.scale, seed=0)
-    # The GPU path's FP64 iteration count is not known here, and a full
-    # solve at 256^3 takes the oracle about 20 minutes: the warm-up measures
-    # the convergence rate between the residuals after 1 and 6 iterations
-    # (at 128^3 it predicts 51 iterations to 1e-10 where the solve takes
-    # 53), the timed steps the time per iteration, and each sample is scaled
-    # to the iterations that rate needs.
+    # A full solve at 256^3 takes the oracle about 15 minutes.  The warm-up
+    # builds the hierarchy once (untimed, as the GPU arm's), runs solves
+    # capped at 1 and 6 iterations: their time difference gives the cost per
+    # iteration and the fixed cost (initial residual, allocations, final true
+    # residual) apart, and their residuals the convergence rate, which
+    # predicts the iterations to 1e-10.  Each timed step is one capped solve
+    # whose iterations are scaled to that count, its fixed cost counted once.
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import Oracle, OracleAmg
     orc = Oracle("orc")
-    samples = []
-    # the hierarchy is built once, outside the timed samples (as the GPU arm's)
-    O = OracleAmg(orc, s, n_coarsest=1000, precision=0, rel_tol=1e-10, max_iter=1)
+    O = OracleAmg(orc, s, n_coarsest=1000, precision=0, rel_tol=wl["rel_tol"], max_iter=1,
+                  **amg_kwargs(wl))
+    t0 = time.perf_counter()
     _, s1 = O.solve(s.b)
+    t1 = time.perf_counter() - t0
     O.set_max_iter(6)
+    t0 = time.perf_counter()
     _, s6 = O.solve(s.b)
+    t6 = time.perf_counter() - t0
+    fixed = max(t1 - (t6 - t1) / 5.0, 0.0)
     iters_needed = s6["n_iter"]
     if not s6["converged"] and s1["n_iter"] == 1 and s6["n_iter"] == 6:
         rate = (s6["final_res"] / s1["final_res"]) ** 0.2
         if 0 < rate < 1:
-            more = np.log(1e-10 * s6["init_res"] / s6["final_res"]) / np.log(rate)
+            more = np.log(wl["rel_tol"] * s6["init_res"] / s6["final_res"]) / np.log(rate)
             iters_needed = 6 + max(0, int(np.ceil(more)))
     O.set_max_iter(args.ref_iters)
+    samples = []
     for step in range(max(args.warmup - 2, 0) + args.steps):
         t0 = time.perf_counter()
         _, st = O.solve(s.b)
         dt = time.perf_counter() - t0
         if step >= args.warmup - 2:
-            samples.append(dt / st["n_iter"] * iters_needed)
+            per_iter = max(dt - fixed, 0.0) / st["n_iter"]
+            samples.append(fixed + per_iter * iters_needed)
     O.close()
     value = statistics.mean(samples)
     line = {"impl": "reference", "metric": "amg_pcg_time_to_1e-10", "value": value, "unit": "s",
@@ -234,81 +288,274 @@ def reference_arm(args, rank, dist):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"{args.workload}: {wl['desc']} (CPU: FP64 V-cycle)",
                        "cells": s.n, "faces": s.nf},
+            "estimate": True,
             "cpu_baseline": {"value": value, "unit": "s", "cores": 1, "kind": "port",
-                             "sample": (f"each step: oracle FP64 AMG-PCG, {args.ref_iters} PCG "
-                                        f"iteration(s) timed, scaled to the {iters_needed} "
-                                        f"iterations to 1e-10 that its convergence rate "
-                                        f"between iterations 1 and 6 gives; hierarchy setup "
-                                        f"untimed")},
+                             "fixed_s": fixed, "per_iteration_s": (t6 - t1) / 5.0,
+                             "iterations_predicted": iters_needed,
+                             "sample": (f"each step: oracle FP64 AMG-PCG solve capped at "
+                                        f"{args.ref_iters} iteration(s); its time less the "
+                                        f"fixed cost ({fixed:.2f} s, from solves capped at 1 "
+                                        f"and 6 iterations) is scaled to the {iters_needed} "
+                                        f"iterations to {wl['rel_tol']:g} that the convergence "
+                                        f"rate between iterations 1 and 6 predicts, and the "
+                                        f"fixed cost added once; hierarchy setup untimed; an "
+                                        f"estimate, not a measured time to solution")},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 4, compare_plain: bool = True):
-    """Config c5 served: a seeded Poisson request stream (200 req/s, sizes
-    log-uniform 8k-2M cells, 60% mixed AMG-PCG / 25% PCG+DIC / 15%
-    PBiCGStab+DILU, tol 1e-8) submitted on its arrival schedule to the
-    continuous-batching server, then the same requests one at a time with
-    the plain FP64 path (FP64 AMG-PCG instead of mixed) on the same GPU.
-    Latency = completion - scheduled arrival."""
+# ---------------------------------------------------------------------------
+# configs c1-c3 beside the headline
+# ---------------------------------------------------------------------------
+def config_block(name: str, steps: int, warmup: int, cpu: bool):
+    """GPU device time, e2e through the reference's C ABI and the oracle's CPU
+    time of one of configs c1-c3 (no hierarchy of the headline is alive)."""
     import torch
     from unap_gb300 import capi
     from unap_gb300 import workloads as W
 
-    reqs = W.serving_requests(count=n_requests, rate=200.0, seed=seed)
-    srv = capi.Server(max_slots=max_slots)
+    cfg = CONFIGS[name]
     t0 = time.perf_counter()
-    ids = []
-    for r in reqs:
-        dt = r.arrival - (time.perf_counter() - t0)
+    s = W.config(name, 1.0, seed=0)
+    gen = time.perf_counter() - t0
+    out = {"desc": cfg["desc"], "cells": s.n, "faces": s.nf, "generate_s": gen}
+    A = capi.DeviceMatrix(s)
+    b = torch.tensor(s.b, device="cuda")
+    x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    peak, _ = hbm_peak()
+    if cfg["kind"] == "krylov":
+        def one():
+            x.zero_()
+            return A.krylov_solve(cfg["method"], cfg["precond"], x, b, rel_tol=cfg["rel_tol"],
+                                  max_iter=5000)
+    else:
+        G = capi.DeviceAmg(A, precision=cfg["precision"], rel_tol=cfg["rel_tol"],
+                           n_coarsest=1000, **amg_kwargs(cfg))
+
+        def one():
+            x.zero_()
+            return G.solve(x, b)
+    for _ in range(warmup):
+        one()
+    st = [one() for _ in range(steps)]
+    if not all(q["converged"] for q in st):
+        raise RuntimeError(f"{name} did not converge: {st[-1]}")
+    out["gpu_s"] = statistics.mean(q["seconds"] for q in st)
+    out["iterations"] = st[-1]["nIterations"]
+    out["true_relative_residual"] = st[-1]["trueResidual"] / st[-1]["initialResidual"] \
+        if st[-1]["trueResidual"] > 0 else None
+    if st[-1]["algorithmicBytes"] > 0:
+        out["whole_solve_gbs"] = st[-1]["algorithmicBytes"] / out["gpu_s"] / 1e9
+    prof = A.profile(reps=10)
+    symm = s.symm
+    k = {"spmv": ("spmv_kernel<double>", spmv64_bytes(s.n, s.nf, symm))}
+    if cfg["kind"] == "krylov":
+        key = "dic_apply" if cfg["precond"] == 2 else "dilu_apply"
+        k[key] = (("dic" if cfg["precond"] == 2 else "dilu") + "_fwd/bwd_kernel",
+                  40 * s.n + (32 if symm else 40) * s.nf)
+    out["kernels"] = {key: {"kernel": nm, "ms": prof[key], "algorithmic_bytes": by,
+                            "achieved_gbs": by / (prof[key] * 1e-3) / 1e9,
+                            "frac": by / (prof[key] * 1e-3) / 1e9 / peak}
+                      for key, (nm, by) in k.items()}
+    # e2e through the reference-facing C ABI with host arrays
+    e2e = []
+    if cfg["kind"] == "krylov":
+        fn = capi.pcgsolversolve if cfg["method"] == 0 else capi.pbicgstabsolversolve
+        for i in range(warmup + steps):
+            t0 = time.perf_counter()
+            h = capi.ldumatrixcreat(s)
+            _, it, _ = fn(np.zeros(s.n), h, s.b, cfg["precond"], rel_tol=cfg["rel_tol"],
+                          max_iter=5000)
+            if i >= warmup:
+                e2e.append(time.perf_counter() - t0)
+        out["e2e"] = {"value": statistics.mean(e2e), "unit": "s",
+                      "call": "ldumatrixcreat_ + " + fn.__name__ + "_ (host arrays, matrix "
+                              "upload and device setup included)",
+                      "h2d_bytes_per_step": 16 * s.n + (16 if symm else 24) * s.nf,
+                      "d2h_bytes_per_step": 8 * s.n}
+    else:
+        xh = np.zeros(s.n)
+        for i in range(warmup + steps):
+            xh[:] = 0
+            t0 = time.perf_counter()
+            G.solve_host(xh, np.ascontiguousarray(s.b))
+            if i >= warmup:
+                e2e.append(time.perf_counter() - t0)
+        out["e2e"] = {"value": statistics.mean(e2e), "unit": "s", "call": "unap_cuda_amg_solve_host",
+                      "h2d_bytes_per_step": 16 * s.n, "d2h_bytes_per_step": 8 * s.n}
+        G.close()
+    A.close()
+    if cpu:
+        try:
+            out["cpu_baseline"] = (oracle_krylov_sample(s, cfg, out["iterations"])
+                                   if cfg["kind"] == "krylov"
+                                   else oracle_amg_sample(s, cfg, out["iterations"], caps=(1, 3)))
+            out["cpu_over_gpu"] = out["cpu_baseline"]["value"] / out["gpu_s"]
+        except Exception as e:  # reported, never fatal
+            out["cpu_baseline"] = {"value": None, "sample": f"failed: {e}"}
+    return out
+
+
+# ---------------------------------------------------------------------------
+# c5: the served stream
+# ---------------------------------------------------------------------------
+class _Builder:
+    """Builds stream requests in a spawn-context process pool (the parent has
+    a CUDA context), at most `window` ahead of the consumer."""
+
+    def __init__(self, specs, window: int, procs: int):
+        import multiprocessing as mp
+        from unap_gb300 import workloads as W
+        self.specs = specs
+        self.pool = mp.get_context("spawn").Pool(procs)
+        self.window = window
+        self.pending = {}
+        self.next_submit = 0
+        self.fn = W.build_request
+        self._fill(0)
+
+    def _fill(self, i):
+        while self.next_submit < len(self.specs) and self.next_submit < i + self.window:
+            j = self.next_submit
+            self.pending[j] = self.pool.apply_async(self.fn, (self.specs[j],))
+            self.next_submit += 1
+
+    def get(self, i):
+        self._fill(i)
+        r = self.pending.pop(i).get()
+        self._fill(i + 1)
+        return r
+
+    def close(self):
+        self.pool.terminate()
+        self.pool.join()
+
+
+def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 12, compare_plain: bool = True,
+                window: int = 64, procs: int = 0):
+    """Config c5 served: the seeded request stream (Poisson arrivals at 200/s,
+    sizes log-uniform 8k-2M cells, 60% mixed AMG-PCG / 25% PCG+DIC / 15%
+    PBiCGStab+DILU, tol 1e-8) submitted on its arrival schedule to the
+    continuous-batching server; then the same requests one at a time through
+    the plain FP64 path (FP64 AMG-PCG instead of mixed).  Latency is counted
+    from each request's scheduled arrival in both: the served requests'
+    completions are measured, the plain path's service times are measured one
+    by one and queued first-in first-out on the same arrival schedule.
+    Request matrices are built by a process pool just ahead of submission;
+    `producer` reports whether the server ever waited for them."""
+    import torch
+    from unap_gb300 import capi
+    from unap_gb300 import workloads as W
+
+    specs = W.serving_stream(count=n_requests, rate=200.0, seed=seed)
+    procs = procs or max(2, min(12, (os.cpu_count() or 4) - 4))
+    srv = capi.Server(max_slots=max_slots)
+    B = _Builder(specs, window, procs)
+    sub_t, ids, ns, inflight_at_late = [], [], [], []
+    results = [None] * len(specs)
+    done_count = [0]
+    lock = threading.Condition()
+
+    def waiter():
+        for i in range(len(specs)):
+            with lock:
+                lock.wait_for(lambda: len(ids) > i)
+                rid, n = ids[i], ns[i]
+            _, info = srv.wait(rid, n)
+            with lock:
+                results[i] = info
+                done_count[0] += 1
+                lock.notify_all()
+
+    th = threading.Thread(target=waiter, daemon=True)
+    th.start()
+    t0 = time.perf_counter()
+    for i, sp in enumerate(specs):
+        r = B.get(i)
+        with lock:  # bounded server queue: at most `window` requests in flight
+            lock.wait_for(lambda: len(ids) - done_count[0] < window)
+        dt = sp.arrival - (time.perf_counter() - t0)
         if dt > 0:
             time.sleep(dt)
-        ids.append(srv.submit(r.system, r.method, rel_tol=1e-8, max_iter=2000))
-    lat, batched, setup, solve_t, queue = [], 0, [], [], []
-    for r, rid in zip(reqs, ids):
-        _, info = srv.wait(rid, r.system.n)
+        now = time.perf_counter() - t0
+        if now > sp.arrival + 0.001:
+            inflight_at_late.append(len(ids) - done_count[0])
+        rid = srv.submit(r.system, r.method, rel_tol=1e-8, max_iter=2000)
+        with lock:
+            sub_t.append(now)
+            ids.append(rid)
+            ns.append(r.system.n)
+            lock.notify_all()
+        del r
+    th.join()
+    srv.close()
+    B.close()
+    lat, setup, solve_t, queue, batched = [], [], [], [], 0
+    for sp, st_, info in zip(specs, sub_t, results):
         if not info["converged"]:
             raise RuntimeError(f"served request did not converge: {info}")
-        lat.append(info["latencySeconds"])
+        lat.append(st_ + info["latencySeconds"] - sp.arrival)
         setup.append(info["setupSeconds"])
         solve_t.append(info["solveSeconds"])
         queue.append(info["queueSeconds"])
         batched += info["batched"]
-    span = time.perf_counter() - t0
-    srv.close()
-
+    last = max(st_ + info["latencySeconds"] for st_, info in zip(sub_t, results))
     pct = lambda v, q: float(np.percentile(np.array(v), q))
     out = {"requests": n_requests, "rate_per_s": 200.0,
-           "solves_per_s": n_requests / span, "p50_s": pct(lat, 50), "p99_s": pct(lat, 99),
+           "solves_per_s": n_requests / (last - specs[0].arrival),
+           "p50_s": pct(lat, 50), "p99_s": pct(lat, 99),
+           "latency": "completion - scheduled arrival (queueing included)",
            "batched_requests": batched, "slots": max_slots,
-           "mean_queue_s": float(np.mean(queue)), "mean_setup_s": float(np.mean(setup)),
-           "mean_solve_s": float(np.mean(solve_t))}
+           "mean_server_queue_s": float(np.mean(queue)), "mean_setup_s": float(np.mean(setup)),
+           "mean_solve_s": float(np.mean(solve_t)),
+           "amg_method": "mixed AMG-PCG, Chebyshev degree 3 V-cycle",
+           "producer": {"build_processes": procs, "window": window,
+                        "submitted_after_arrival": len(inflight_at_late),
+                        "min_in_flight_then": min(inflight_at_late) if inflight_at_late else None,
+                        "note": "the server was never short of work when min_in_flight_then "
+                                "exceeds the slots"}}
     if not compare_plain:
         return out
     # the plain path: one request at a time, FP64 everywhere
-    seq_lat = []
-    t1 = time.perf_counter()
-    for r in reqs:
-        ts = time.perf_counter()
-        s = r.system
-        A = capi.DeviceMatrix(s)
-        x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
-        b = torch.tensor(s.b, device="cuda")
-        if r.method == "amg_mixed":
-            G = capi.DeviceAmg(A, precision=0, rel_tol=1e-8, max_iter=2000)
-            G.solve(x, b)
-            G.close()
-        else:
-            A.krylov_solve(0 if r.method == "pcg_dic" else 1, 2 if r.method == "pcg_dic" else 3,
-                           x, b, rel_tol=1e-8, max_iter=2000)
-        _ = x.cpu()
-        A.close()
-        seq_lat.append(time.perf_counter() - ts)
-    seq_span = time.perf_counter() - t1
-    out["one_at_a_time_fp64"] = {"solves_per_s": n_requests / seq_span,
-                                 "p50_s": pct(seq_lat, 50), "p99_s": pct(seq_lat, 99),
-                                 "latency": "solve time alone, no queueing"}
+    B = _Builder(specs, 16, procs)
+    svc = []
+    try:
+        for i, sp in enumerate(specs):
+            r = B.get(i)
+            s = r.system
+            b = torch.tensor(s.b, device="cuda")
+            torch.cuda.synchronize()
+            ts = time.perf_counter()
+            A = capi.DeviceMatrix(s)
+            x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+            if r.method == "amg_mixed":
+                G = capi.DeviceAmg(A, precision=0, rel_tol=1e-8, max_iter=2000,
+                                   smoother=1, cheby_degree=3, cheby_from=0, eig_ratio=30.0)
+                st = G.solve(x, b)
+                G.close()
+            else:
+                st = A.krylov_solve(0 if r.method == "pcg_dic" else 1,
+                                    2 if r.method == "pcg_dic" else 3, x, b, rel_tol=1e-8,
+                                    max_iter=2000)
+            _ = x.cpu()
+            A.close()
+            svc.append(time.perf_counter() - ts)
+            if not st["converged"]:
+                raise RuntimeError(f"plain request did not converge: {st}")
+    finally:
+        B.close()
+    c, qlat = 0.0, []
+    for sp, dt in zip(specs, svc):
+        c = max(c, sp.arrival) + dt
+        qlat.append(c - sp.arrival)
+    out["one_at_a_time_fp64"] = {
+        "solves_per_s": n_requests / (c - specs[0].arrival),
+        "p50_s": pct(qlat, 50), "p99_s": pct(qlat, 99),
+        "latency": "first-in first-out on the same arrival schedule: completion - scheduled "
+                   "arrival, from each request's measured service time",
+        "service_p50_s": pct(svc, 50), "service_p99_s": pct(svc, 99),
+        "amg_method": "FP64 AMG-PCG, Chebyshev degree 3 V-cycle"}
     return out
 
 
@@ -434,6 +681,42 @@ def setup_case(args):
     print(json.dumps(out), flush=True)
 
 
+def smoother_roofline(G, info, mixed: bool, peak: float, deg: int):
+    """Per-level smoother launch groups of the V-cycle timed with CUDA events
+    (unap_cuda_amg_profile_smoother), and the kernel family with the largest
+    device time per V-cycle: Chebyshev steps (2 deg - 1 launches per level
+    and V-cycle: the first pre-smoothing step runs inside the restriction)
+    or Gauss-Seidel sweeps (nPre + nPost = 4 per level)."""
+    fam = {"cheb": {"ms": 0.0, "bytes": 0.0, "levels": []},
+           "gs_fine": {"ms": 0.0, "bytes": 0.0, "levels": []},
+           "gs_coarse": {"ms": 0.0, "bytes": 0.0, "levels": []}}
+    lam = G.eigenvalues()
+    per_level = []
+    for k in range(info["n_levels"] - 1):
+        ms, by, launches = G.profile_smoother(k, reps=10)
+        cheb = lam[k] > 0
+        reps = (2 * deg - 1) if cheb else 4
+        f = "cheb" if cheb else ("gs_fine" if k == 0 else "gs_coarse")
+        fam[f]["ms"] += reps * ms
+        fam[f]["bytes"] += reps * by
+        fam[f]["levels"].append(k)
+        per_level.append({"level": k, "smoother": "chebyshev" if cheb else "gauss-seidel",
+                          "ms": ms, "launches": launches, "algorithmic_bytes": by,
+                          "achieved_gbs": by / (ms * 1e-3) / 1e9})
+    names = {"cheb": "cheb_step_kernel<%s>" % ("float" if mixed else "double"),
+             "gs_fine": "gs_kernel<%s>" % ("float" if mixed else "double"),
+             "gs_coarse": "gs_packed_kernel<%s>" % ("float" if mixed else "double")}
+    groups = {}
+    for f, v in fam.items():
+        if v["ms"] > 0:
+            ach = v["bytes"] / (v["ms"] * 1e-3) / 1e9
+            groups[f] = {"kernel": names[f], "levels": v["levels"], "ms_per_vcycle": v["ms"],
+                         "algorithmic_bytes_per_vcycle": v["bytes"], "achieved": ach,
+                         "frac": ach / peak}
+    top = max(groups, key=lambda f: groups[f]["ms_per_vcycle"])
+    return top, groups, per_level
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -443,9 +726,12 @@ def main():
     ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS))
     ap.add_argument("--scale", type=float, default=1.0, help="grid edge scale (testing)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the c1-c3 blocks")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the all-Gauss-Seidel V-cycle comparison")
     ap.add_argument("--ref-iters", type=int, default=1,
                     help="PCG iterations per reference-arm sample")
-    ap.add_argument("--serve", type=int, default=200,
+    ap.add_argument("--serve", type=int, default=2000,
                     help="also serve this many requests of the c5 stream (rank 0 of a "
                          "1-GPU run; 0: skip)")
     ap.add_argument("--serve-slots", type=int, default=12,
@@ -490,14 +776,10 @@ def main():
     wl = WORKLOADS[args.workload]
     s = W.config(args.workload, args.scale, seed=rank)
     A = capi.DeviceMatrix(s)
-    G = capi.DeviceAmg(A, precision=wl["precision"], rel_tol=1e-10, n_coarsest=1000)
-    G64 = capi.DeviceAmg(A, precision=0, rel_tol=1e-10, n_coarsest=1000) \
-        if wl["precision"] == 1 else G
+    mixed = wl["precision"] == 1
+    kw = amg_kwargs(wl)
+    G = capi.DeviceAmg(A, precision=wl["precision"], rel_tol=wl["rel_tol"], n_coarsest=1000, **kw)
     info = G.info()
-    tail_rows, single_rows = capi.get_tail_rows(wl["precision"])
-    tail_info = {"cluster_ctas": capi.tail_cluster_size(), "tail_rows": tail_rows,
-                 "single_cta_rows": single_rows,
-                 "levels_in_tail": sum(1 for c in info["cells"][:-1] if c <= tail_rows)}
     b = torch.tensor(s.b, device=device)
     x = torch.zeros(s.n, dtype=torch.float64, device=device)
 
@@ -532,21 +814,7 @@ def main():
     per_solve = max_over_ranks(statistics.mean(dev_s), dist, device)
     iters = stats[-1]["nIterations"]
     true_rel = stats[-1]["trueResidual"] / stats[-1]["initialResidual"]
-
-    # FP64 AMG-PCG on the same matrix (the metric's "mixed vs FP64")
-    fp64 = None
-    if G64 is not G:
-        x_mixed = x.clone()
-        for _ in range(args.warmup):
-            solve(G64)
-        st64 = [solve(G64) for _ in range(args.steps)]
-        t64 = max_over_ranks(statistics.mean(st["seconds"] for st in st64), dist, device)
-        # the mixed solution against the FP64 one (both to a 1e-10 residual)
-        rel = float(torch.linalg.vector_norm(x_mixed - x) / torch.linalg.vector_norm(x))
-        fp64 = {"value": t64, "unit": "s", "iterations": st64[-1]["nIterations"],
-                "speedup_mixed_vs_fp64": t64 / per_solve,
-                "mixed_solution_rel_diff_vs_fp64": rel}
-    gpu_iters64 = fp64["iterations"] if fp64 else iters
+    x_head = x.clone()
 
     # e2e: the host-array C ABI call, b/x copies inside the timed region
     xh = torch.zeros(s.n, dtype=torch.float64).pin_memory()
@@ -563,70 +831,101 @@ def main():
         e2e_t.append(time.perf_counter() - t0)
     e2e_v = max_over_ranks(statistics.mean(e2e_t), dist, device)
 
-    # roofline of the dominant kernel: the FP32 (FP64) Gauss-Seidel sweep of
-    # the finest level, all wavefront launches of one sweep timed with CUDA
-    # events on the matrix's stream.  The whole solve's algorithmic bytes
-    # (the library's per-step bookkeeping) over its device time are reported
-    # beside it, with the FP64 SpMV.
-    prof = A.profile(reps=10)
+    # roofline: the smoother kernel family with the largest device time per
+    # V-cycle, from per-level launch groups timed with CUDA events
     peak, peak_kind = hbm_peak()
     peak_src = ("measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                 else "fallback 6.8 TB/s")
-    mixed = wl["precision"] == 1
-    sweep_bytes = gs32_sweep_bytes(s.n, s.nf) if mixed else 32 * s.n + 16 * s.nf
-    sweep_ms = prof["gs_fwd32"] if mixed else prof["gs_fwd"]
-    achieved = sweep_bytes / (sweep_ms * 1e-3) / 1e9
-    spmv = {"kernel": "spmv_kernel<double>", "ms": prof["spmv"],
-            "achieved": spmv64_bytes(s.n, s.nf) / (prof["spmv"] * 1e-3) / 1e9}
+    deg = kw.get("cheby_degree", 3)
+    top, groups, per_level = smoother_roofline(G, info, mixed, peak, deg)
+    vprof = G.profile_vcycle(reps=10)
+    mprof = A.profile(reps=10)
+    spmv = {"kernel": "spmv_kernel<double>", "ms": mprof["spmv"],
+            "achieved": spmv64_bytes(s.n, s.nf) / (mprof["spmv"] * 1e-3) / 1e9}
+    spmv["frac"] = spmv["achieved"] / peak
     solve_bytes = stats[-1].get("algorithmicBytes", 0.0)
     whole = None
     if solve_bytes > 0:
         whole = {"algorithmic_bytes": solve_bytes, "s": statistics.mean(dev_s),
                  "achieved": solve_bytes / statistics.mean(dev_s) / 1e9}
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak,
-                "traffic": SWEEP_TRAFFIC_RATIO * sweep_bytes if mixed else None,
-                "traffic_source": "in-situ DRAM bytes of a whole FP32 sweep measured by ncu "
-                                  "on the 192^3 case (profiles/gs_kernel_float_c4_192cube_"
-                                  "waves.md), ratio 1.29 to algorithmic, scaled to this sweep"
-                                  if mixed else None,
-                "kernel": "gs_kernel<float>" if mixed else "gs_kernel<double>",
-                "launch_group": f"one forward sweep of the finest level "
-                                f"({A.info()['n_wavefronts']} wavefront launches)",
-                "algorithmic_bytes_per_sweep": sweep_bytes, "sweep_ms": sweep_ms,
-                "peak_source": peak_src, "spmv64": spmv, "whole_solve": whole}
+        whole["frac"] = whole["achieved"] / peak
+    tg = groups[top]
+    roofline = {"bound": "hbm", "achieved": tg["achieved"], "peak": peak, "unit": "GB/s",
+                "frac": tg["achieved"] / peak, "traffic": None,
+                "kernel": tg["kernel"], "levels": tg["levels"],
+                "launch_group": ("every launch of this kernel in one V-cycle, each level's "
+                                 "launch group timed alone with CUDA events on the matrix's "
+                                 "stream (inputs larger than L2 on the largest levels)"),
+                "ms_per_vcycle": tg["ms_per_vcycle"],
+                "algorithmic_bytes_per_vcycle": tg["algorithmic_bytes_per_vcycle"],
+                "peak_source": peak_src, "groups": groups, "per_level": per_level,
+                "vcycle_ms": vprof["vcycle_ms"], "vcycle_level_ms": vprof["level_ms"],
+                "spmv64": spmv, "whole_solve": whole}
 
-    # the kernels with the largest share of device time: the V-cycle's
-    # sweeps on levels 1..L-1 (row-packed, one launch per wavefront; the
-    # smallest levels run in the one-CTA tail), from the per-level profile
-    # of a graph-captured V-cycle; algorithmic bytes per level = 4 sweeps and
-    # one residual of (16 N + 12 F) for FP32 rows (8 x 4 bytes for FP64)
-    prof = G.profile_vcycle(reps=10)
-    lsz = G.level_sizes()
-    lvl_ms = prof["level_ms"]
-    cb, fb = (16.0, 12.0) if mixed else (32.0, 16.0)
-    coarse_bytes = sum(5 * (cb * n + fb * f) for (n, f, _) in lsz[1:-1])
-    coarse_ms = sum(lvl_ms[1:len(lsz) - 1]) + (lvl_ms[len(lsz) - 1] if len(lvl_ms) >= len(lsz)
-                                               else 0.0)
-    coarse_gbs = coarse_bytes / (coarse_ms * 1e-3) / 1e9 if coarse_ms > 0 else None
-    roofline["coarse_levels"] = {
-        "kernel": "gs_packed_kernel<float>" if mixed else "gs_packed_kernel<double>",
-        "levels": f"1-{len(lsz) - 1} (with the coarsest dense solve)",
-        "share_of_vcycle": coarse_ms / prof["vcycle_ms"] if prof["vcycle_ms"] else None,
-        "vcycle_ms": prof["vcycle_ms"], "level_ms": lvl_ms[:len(lsz)],
-        "wavefronts_per_level": [w for (_, _, w) in lsz],
-        "algorithmic_bytes": coarse_bytes, "ms": coarse_ms,
-        "achieved": coarse_gbs, "unit": "GB/s",
-        "frac": coarse_gbs / peak if coarse_gbs else None,
-        "bound": "latency: one dependent launch per wavefront (about 2,000 per V-cycle)"}
+    # the same V-cycle in FP64, and the all-Gauss-Seidel V-cycle in both
+    # precisions (the metric's "mixed vs FP64")
+    fp64 = None
+    smoothers = {}
+    variants = []
+    if mixed:
+        variants.append(("fp64", 0, kw))
+    if not args.no_compare and kw.get("smoother", 0) == 1:
+        variants += [("gs_mixed", 1, {}), ("gs_fp64", 0, {})] if mixed else [("gs_fp64", 0, {})]
+    x_fp64 = None
+    for name, prec, vkw in variants:
+        H = capi.DeviceAmg(A, precision=prec, rel_tol=wl["rel_tol"], n_coarsest=1000, **vkw)
+        nsteps = args.steps if name == "fp64" else 2
+        for _ in range(args.warmup if name == "fp64" else 1):
+            solve(H)
+        sts = [solve(H) for _ in range(nsteps)]
+        t = max_over_ranks(statistics.mean(q["seconds"] for q in sts), dist, device)
+        vp = H.profile_vcycle(reps=5)
+        smoothers[name] = {"value": t, "unit": "s", "iterations": sts[-1]["nIterations"],
+                           "precision": "fp32 V-cycle" if prec else "fp64",
+                           "smoother": "chebyshev" if vkw.get("smoother") else "gauss-seidel",
+                           "vcycle_ms": vp["vcycle_ms"], "level_ms": vp["level_ms"]}
+        if name == "fp64":
+            x_fp64 = x.clone()
+        H.close()
+    if mixed:
+        f = smoothers.pop("fp64")
+        rel = float(torch.linalg.vector_norm(x_head - x_fp64) / torch.linalg.vector_norm(x_fp64))
+        fp64 = {"value": f["value"], "unit": "s", "iterations": f["iterations"],
+                "speedup_mixed_vs_fp64": f["value"] / per_solve,
+                "mixed_solution_rel_diff_vs_fp64": rel,
+                "fp64_pinned_by": "the FP64 GPU AMG-PCG matches the oracle at full 128^3 (c2, "
+                                  "+-1 iteration, solution within 1e-10 at relTol 1e-13) in "
+                                  "tests/test_gpu_fullsize.py",
+                "vcycle_ms": f["vcycle_ms"]}
+    smoothers["headline"] = {"value": per_solve, "unit": "s", "iterations": iters,
+                             "precision": "fp32 V-cycle" if mixed else "fp64",
+                             "smoother": "chebyshev" if kw.get("smoother") else "gauss-seidel",
+                             "vcycle_ms": vprof["vcycle_ms"], "level_ms": vprof["level_ms"]}
+    gpu_iters64 = fp64["iterations"] if fp64 else iters
+    G.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_baseline(s, gpu_iters64)
+            cpu = oracle_amg_sample(s, wl, gpu_iters64)
         except Exception as e:  # reported, never fatal
             cpu = {"value": None, "unit": "s", "cores": 1, "kind": "port",
                    "sample": f"failed: {e}"}
+    matrix_bytes = A.info()["device_bytes"]
+    A.close()
+    del b, x, x_head, x_fp64
+    torch.cuda.empty_cache()
+
+    configs = None
+    if rank == 0 and world == 1 and not args.no_configs and args.workload == "c4":
+        configs = {}
+        for name in ("c1", "c2", "c3"):
+            try:
+                configs[name] = config_block(name, args.steps, args.warmup,
+                                             cpu=not args.no_cpu_baseline)
+            except Exception as e:  # reported in the line, never fatal
+                configs[name] = {"error": str(e)}
+            torch.cuda.empty_cache()
 
     serving = None
     if args.serve > 0 and rank == 0 and world == 1:
@@ -635,7 +934,6 @@ def main():
         except Exception as e:  # reported in the line, never fatal
             serving = {"error": str(e)}
 
-    matrix_bytes = A.info()["device_bytes"]
     line = {
         "metric": "amg_pcg_time_to_1e-10",
         "value": per_solve,
@@ -647,18 +945,19 @@ def main():
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64 outer PCG + f32 V-cycle" if wl["precision"] == 1 else "f64",
+        "dtype": "f64 outer PCG + f32 V-cycle" if mixed else "f64",
         "data": "synthetic (seeded generator; the reference ships no data sets)",
         "config": {"workload": f"{args.workload}: {wl['desc']}", "cells": s.n, "faces": s.nf,
                    "levels": info["n_levels"], "level_cells": info["cells"],
                    "coarsest": info["cells"][-1], "iterations": iters,
-                   "true_relative_residual": true_rel,
+                   "true_relative_residual": true_rel, "vcycle": kw,
                    "l2": f"inputs larger than L2: matrix {matrix_bytes / 1e9:.2f} GB on device "
                          f"> {L2_BYTES / 1e6:.0f} MB",
                    "setup_s": info["setup_s"], "wall_s_per_step": t_wall / args.steps,
-                   "vcycle_tail": tail_info,
                    "parallelism": f"replicas x{world}"},
         "fp64": fp64,
+        "smoothers": smoothers,
+        "configs": configs,
         "serving": serving,
         "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": 2 * 8 * s.n,
                 "d2h_bytes_per_step": 8 * s.n},
@@ -669,10 +968,6 @@ def main():
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    G.close()
-    if G64 is not G:
-        G64.close()
-    A.close()
     if dist is not None:
         dist.destroy_process_group()
 

@@ -125,6 +125,22 @@ void sw_solve_pbicgstab__(long int* solverPtrPtr, long int* APtrPtr, double* xPt
 void sw_matrix_destroy__(long int* APtrPtr);
 void sw_solver_destroy_pbicgstab__(long int* solverPtrPtr);
 
+/* COO / face reordering (fortranInterface.hpp:110-145, defined in
+ * fortranInterface.cpp:467-534 over matrixConversion.cpp:38-222), 1-based
+ * row and column indices on entry, 0-based on return.  reordercoo_ groups
+ * the entries by row and orders each row by column, moving the values with
+ * them (it shifts to 0-based only when row[0] != 0, as the reference does);
+ * reorderuface__ does the same to the indices alone and returns each
+ * entry's new position in newOrder (0-based); reorderlface__ groups them by
+ * column, stable in input order, with newOrder likewise; reordervalue__
+ * moves val[i] to val[newOrder[i]].  Input the reference leaves undefined
+ * (an index out of range, a repeated (row, column) pair, a newOrder that is
+ * not a permutation) leaves the arrays unchanged and prints the error. */
+void reordercoo_(double* val, int* row, int* col, int* nCellsPtr, int* sizePtr);
+void reorderuface__(int* row, int* col, int* nCellsPtr, int* sizePtr, int* newOrder);
+void reorderlface__(int* row, int* col, int* nCellsPtr, int* sizePtr, int* newOrder);
+void reordervalue__(double* val, int* newOrder, int* sizePtr);
+
 /* ===================================================================== */
 /* Part 2: GB300 entry points (no counterpart in the reference)          */
 /* ===================================================================== */
@@ -159,6 +175,10 @@ int unap_cuda_matrix_create(long int* handle, int nCells, int nFaces, const int*
                             const int* upperAddr, const double* lower, const double* diag,
                             const double* upper);
 int unap_cuda_matrix_destroy(long int handle);
+/* Replace a matrix's coefficients, keeping its addressing and its symmetry
+ * (lower NULL or == upper for a symmetric matrix). */
+int unap_cuda_matrix_set_values(long int handle, const double* diag, const double* upper,
+                                const double* lower);
 /* Sizes and host copy of a handle's LDU arrays (any handle from Part 1 or
  * Part 2; no GPU work).  lower receives upper's values when symmetric. */
 int unap_cuda_matrix_size(long int handle, int* nCells, int* nFaces, int* symm);
@@ -196,6 +216,52 @@ int unap_cuda_spmv(long int handle, const double* x, double* y);
 int unap_cuda_spmv_noalloc(long int handle, const double* x, double* y);
 /* w = M^-1 r, precond 1 Diag, 2 DIC, 3 DILU */
 int unap_cuda_precondition(long int handle, int precond, const double* r, double* w);
+
+/* The same calls on HOST vectors in the caller's cell order: each copies its
+ * vectors to the device, runs the kernels there and copies the result back
+ * (the layer under the C++ class API, include/unap/).  No counterpart in the
+ * reference, which works on host vectors throughout. */
+int unap_cuda_spmv_host(long int handle, const double* x, double* y);
+int unap_cuda_precondition_host(long int handle, int precond, const double* r, double* w);
+/* rD of lduDiagPrecond (1), lduDICPrecond (2) or lduDILUPrecond (3) in cell
+ * order (lduDiagPrecond.cpp:13-41, lduDICPrecond.cpp:15-42,
+ * lduDILUPrecond.cpp:15-43), computed on the device */
+int unap_cuda_precond_rD(long int handle, int precond, double* rD);
+int unap_cuda_gauss_seidel_host(long int handle, double* x, const double* b, int nSweeps,
+                                int backward);
+/* chebySmoother::smooth (chebySmoother.cpp:13-149) with its state held by
+ * the caller: while *estimated is 0 the call estimates the largest
+ * eigenvalue with 10 diagonal-PCG iterations on (x, b), leaving x as they
+ * change it, stores it in *maxEig and sets *estimated; later calls run
+ * nSweeps (<= 16) Chebyshev steps over [maxEig / 1.5, 1.1 maxEig]. */
+int unap_cuda_cheby_smooth_host(long int handle, double* x, const double* b, int nSweeps,
+                                double* maxEig, int* estimated);
+int unap_cuda_krylov_solve_host(long int handle, int method, int precond, double tol,
+                                double relTol, int maxIter, int minIter, double* x,
+                                const double* b, unap_cuda_stats* stats);
+
+/* 0-based forms of the reordering calls above (matrixConversion.cpp:38-222);
+ * they return UNAP_CUDA_EINVAL on the inputs listed there. */
+int unap_cuda_reorder_coo(double* val, int* row, int* col, int nCells, int size);
+int unap_cuda_reorder_uface(int* row, int* col, int nCells, int size, int* newOrder);
+int unap_cuda_reorder_lface(int* row, int* col, int nCells, int size, int* newOrder);
+int unap_cuda_reorder_value(double* val, const int* newOrder, int size);
+
+/* Pairwise agglomeration of a matrix (lduAgglomeration::agglomerate,
+ * lduAgglomerate.cpp:4-271 with lduAgglomerationAddressing.cpp:8-178 and
+ * lduAgglomerateMatrix.cpp:3-131): face weights as given (the C++ API's
+ * agglomerate(weights)), levels kept while they have at least
+ * nCellsInCoarsestLevel cells, at most maxLevels.  _level copies level k's
+ * arrays (any pointer may be NULL): restrictAddr (finer cells -> cells of
+ * level k), faceRestrict (finer faces -> coarse face or -(cell + 1)), and
+ * the level's LDU matrix. */
+int unap_cuda_agglomeration_create(long int* aggl, long int matrix, const double* weights,
+                                   int nCellsInCoarsestLevel, int maxLevels);
+int unap_cuda_agglomeration_size(long int aggl, int* nLevels);
+int unap_cuda_agglomeration_level(long int aggl, int level, int* nCells, int* nFaces, int* symm,
+                                  int* restrictAddr, int* faceRestrict, int* lowerAddr,
+                                  int* upperAddr, double* diag, double* upper, double* lower);
+int unap_cuda_agglomeration_destroy(long int aggl);
 /* nSweeps Gauss-Seidel sweeps in place on x; backward != 0 sweeps in reverse
  * cell order (no reference counterpart) */
 int unap_cuda_gauss_seidel(long int handle, double* x, const double* b, int nSweeps,
@@ -264,6 +330,14 @@ int unap_cuda_amg_vcycle(long int amg, const double* r, double* z);
  * the levels below it 0).  *written = entries filled.  No counterpart in the
  * reference. */
 int unap_cuda_amg_profile_vcycle(long int amg, int reps, double* ms, int maxOut, int* written);
+/* Mean device time (CUDA events on the handle's stream) of one smoothing
+ * launch group on AMG level `level` (not the coarsest), in the V-cycle's
+ * precision, on scratch vectors: one Chebyshev step on a Chebyshev level,
+ * one forward Gauss-Seidel sweep (a launch per wavefront) otherwise.
+ * *bytes = its algorithmic DRAM bytes, *launches = kernel launches per
+ * group.  No counterpart in the reference. */
+int unap_cuda_amg_profile_smoother(long int amg, int level, int reps, double* ms, double* bytes,
+                                   int* launches);
 /* The Chebyshev smoother's eigenvalue estimate of every level but the
  * coarsest (0 on Gauss-Seidel levels): lam[k] for k < min(nLevels - 1,
  * maxOut); *written = entries filled.  No counterpart in the reference. */
@@ -283,6 +357,12 @@ int unap_cuda_mg_create(long int* mg, long int matrix, const double* weights, in
 /* number of coarse levels; cells[k] for k <= nCoarseLevels (k = 0 finest) */
 int unap_cuda_mg_levels(long int mg, int* nCoarseLevels, int* cells, int maxOut);
 int unap_cuda_mg_solve(long int mg, double* x, const double* b, unap_cuda_stats* stats);
+/* the same on host vectors (copied to the device and back) */
+int unap_cuda_mg_solve_host(long int mg, double* x, const double* b, unap_cuda_stats* stats);
+/* MGSolver setters after creation (MG.cpp:22-53): nPre/nPost/nFinest
+ * sweeps, correction scaling (0/1), tol, relTol, maxIter, minIter */
+int unap_cuda_mg_set(long int mg, int nPre, int nPost, int nFinest, int scaleCorr, double tol,
+                     double relTol, int maxIter, int minIter);
 int unap_cuda_mg_destroy(long int mg);
 
 /* ---- Batched solves of many systems of uneven size.  Systems of at most
@@ -308,7 +388,8 @@ int unap_cuda_batch_destroy(long int batch);
 
 /* ---- Continuous-batching solve server.  Requests carry their own matrix
  * (host arrays, copied) and right-hand side; method 0 mixed AMG-PCG, 1 FP64
- * AMG-PCG, 2 PCG+DIC, 3 PBiCGStab+DILU.  A request is admitted when a slot
+ * AMG-PCG (both with the Chebyshev degree-3 V-cycle on every level,
+ * eigRatio 30), 2 PCG+DIC, 3 PBiCGStab+DILU.  A request is admitted when a slot
  * is free and its device-memory estimate fits what the solves in flight
  * leave of memoryBudget (0: 80% of free memory); maxSlots large solves run
  * on their own streams so their work overlaps on the GPU; PCG/PBiCGStab

@@ -409,4 +409,36 @@ int ref_read_interfaces(const char* path, int* nNei, int* nFaces, int* neighbour
     return 0;
 }
 
+/* matrixConversion.cpp:38-222, 0-based: the reference's reorderings on
+ * label copies of the caller's int arrays */
+void ref_reorder_coo(double* val, int* row, int* col, int n, int size)
+{
+    std::vector<label> r(row, row + size), c(col, col + size);
+    reorderCOO(val, r.data(), c.data(), n, size);
+    for (int i = 0; i < size; ++i) {
+        row[i] = (int)r[(size_t)i];
+        col[i] = (int)c[(size_t)i];
+    }
+}
+
+void ref_reorder_faces(int byColumn, int* row, int* col, int n, int size, int* newOrder)
+{
+    std::vector<label> r(row, row + size), c(col, col + size), o((size_t)size);
+    if (byColumn)
+        reorderLFace(r.data(), c.data(), n, size, o.data());
+    else
+        reorderUFace(r.data(), c.data(), n, size, o.data());
+    for (int i = 0; i < size; ++i) {
+        row[i] = (int)r[(size_t)i];
+        col[i] = (int)c[(size_t)i];
+        newOrder[i] = (int)o[(size_t)i];
+    }
+}
+
+void ref_reorder_value(double* val, const int* newOrder, int size)
+{
+    std::vector<label> o(newOrder, newOrder + size);
+    reorderValue(val, o.data(), size);
+}
+
 }  // extern "C"

@@ -178,3 +178,83 @@ int main(void)
     run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert run.returncode == 0, (run.stdout, run.stderr)
     assert "sm_103a" in run.stdout
+
+
+def _coo_case(rng, n, density):
+    """A structurally symmetric COO pattern, grouped by row, each row's
+    entries in random column order (the reordering's input)."""
+    rows, cols = [], []
+    for r in range(n):
+        cs = [c for c in range(n) if c == r or rng.random() < density]
+        rng.shuffle(cs)
+        rows += [r] * len(cs)
+        cols += cs
+    return (np.array(rows, np.int32), np.array(cols, np.int32),
+            rng.standard_normal(len(rows)))
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def test_reorder_entry_points_against_reference():
+    """reordercoo_/reorderuface__/reorderlface__/reordervalue__ and their
+    0-based forms give the reference's matrixConversion results bit for bit
+    (where the reference build exists), and a sorted-order check everywhere."""
+    from oracle_lib import Oracle, ref_available
+    lib = capi.load()
+    ref = Oracle("ref").lib if ref_available() else None
+    rng = np.random.default_rng(4)
+    for n, dens in ((1, 0.0), (7, 0.3), (40, 0.1), (200, 0.02)):
+        r0, c0, v0 = _coo_case(rng, n, dens)
+        size = len(r0)
+        # reordercoo_ (1-based in)
+        r, c, v = (r0 + 1).copy(), (c0 + 1).copy(), v0.copy()
+        lib.reordercoo_(_dp(v), _ip(r), _ip(c),
+                        ctypes.byref(ctypes.c_int(n)), ctypes.byref(ctypes.c_int(size)))
+        key = r.astype(np.int64) * n + c
+        assert np.all(np.diff(key) > 0)
+        order = np.lexsort((c0, r0))
+        assert np.array_equal(v, v0[order]) and np.array_equal(r, r0[order])
+        if ref is not None:
+            rr, cr, vr = r0.copy(), c0.copy(), v0.copy()
+            ref.ref_reorder_coo(vr.ctypes.data, rr.ctypes.data, cr.ctypes.data, n, size)
+            assert np.array_equal(rr, r) and np.array_equal(cr, c) and np.array_equal(vr, v)
+        for by_col, fn in ((0, lib.reorderuface__), (1, lib.reorderlface__)):
+            r, c, o = (r0 + 1).copy(), (c0 + 1).copy(), np.zeros(size, np.int32)
+            fn(_ip(r), _ip(c), ctypes.byref(ctypes.c_int(n)), ctypes.byref(ctypes.c_int(size)),
+               _ip(o))
+            assert np.array_equal(np.sort(o), np.arange(size))
+            if ref is not None:
+                rr, cr, orr = r0.copy(), c0.copy(), np.zeros(size, np.int32)
+                ref.ref_reorder_faces(by_col, rr.ctypes.data, cr.ctypes.data, n, size,
+                                      orr.ctypes.data)
+                assert np.array_equal(rr, r) and np.array_equal(cr, c) and np.array_equal(orr, o)
+            vals = v0.copy()
+            lib.reordervalue__(_dp(vals), _ip(o), ctypes.byref(ctypes.c_int(size)))
+            assert np.array_equal(vals[o], v0)
+            if ref is not None:
+                vr = v0.copy()
+                ref.ref_reorder_value(vr.ctypes.data, o.ctypes.data, size)
+                assert np.array_equal(vr, vals)
+
+
+def test_reorder_rejects_undefined_input():
+    """A repeated (row, column) pair or an index out of range: the arrays
+    stay as they were and the 0-based call returns UNAP_CUDA_EINVAL."""
+    lib = capi.load()
+    r = np.array([0, 0, 1], np.int32)
+    c = np.array([1, 1, 0], np.int32)
+    v = np.array([1.0, 2.0, 3.0])
+    before = (r.copy(), c.copy(), v.copy())
+    assert lib.unap_cuda_reorder_coo(v.ctypes.data, r.ctypes.data, c.ctypes.data, 2, 3) == -1
+    assert all(np.array_equal(a, b) for a, b in zip((r, c, v), before))
+    c2 = np.array([1, 5, 0], np.int32)
+    o = np.zeros(3, np.int32)
+    assert lib.unap_cuda_reorder_lface(r.ctypes.data, c2.ctypes.data, 2, 3, o.ctypes.data) == -1
+    assert lib.unap_cuda_reorder_value(v.ctypes.data, np.array([0, 0, 1], np.int32).ctypes.data,
+                                       3) == -1

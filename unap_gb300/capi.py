@@ -64,6 +64,30 @@ SIGNATURES = {
     "sw_solve_pbicgstab__": (None, [_lp, _lp, _dp, _dp, _dp]),
     "sw_matrix_destroy__": (None, [_lp]),
     "sw_solver_destroy_pbicgstab__": (None, [_lp]),
+    "reordercoo_": (None, [_dp, _ip, _ip, _ip, _ip]),
+    "reorderuface__": (None, [_ip, _ip, _ip, _ip, _ip]),
+    "reorderlface__": (None, [_ip, _ip, _ip, _ip, _ip]),
+    "reordervalue__": (None, [_dp, _ip, _ip]),
+    "unap_cuda_matrix_set_values": (_c_int, [_c_long, _vp, _vp, _vp]),
+    "unap_cuda_spmv_host": (_c_int, [_c_long, _vp, _vp]),
+    "unap_cuda_precondition_host": (_c_int, [_c_long, _c_int, _vp, _vp]),
+    "unap_cuda_precond_rD": (_c_int, [_c_long, _c_int, _vp]),
+    "unap_cuda_gauss_seidel_host": (_c_int, [_c_long, _vp, _vp, _c_int, _c_int]),
+    "unap_cuda_cheby_smooth_host": (_c_int, [_c_long, _vp, _vp, _c_int, _vp, _vp]),
+    "unap_cuda_krylov_solve_host": (_c_int, [_c_long, _c_int, _c_int, _c_dbl, _c_dbl, _c_int,
+                                             _c_int, _vp, _vp, ctypes.POINTER(Stats)]),
+    "unap_cuda_reorder_coo": (_c_int, [_vp, _vp, _vp, _c_int, _c_int]),
+    "unap_cuda_reorder_uface": (_c_int, [_vp, _vp, _c_int, _c_int, _vp]),
+    "unap_cuda_reorder_lface": (_c_int, [_vp, _vp, _c_int, _c_int, _vp]),
+    "unap_cuda_reorder_value": (_c_int, [_vp, _vp, _c_int]),
+    "unap_cuda_agglomeration_create": (_c_int, [_lp, _c_long, _vp, _c_int, _c_int]),
+    "unap_cuda_agglomeration_size": (_c_int, [_c_long, _vp]),
+    "unap_cuda_agglomeration_level": (_c_int, [_c_long, _c_int, _vp, _vp, _vp, _vp, _vp, _vp,
+                                               _vp, _vp, _vp, _vp]),
+    "unap_cuda_agglomeration_destroy": (_c_int, [_c_long]),
+    "unap_cuda_mg_solve_host": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
+    "unap_cuda_mg_set": (_c_int, [_c_long, _c_int, _c_int, _c_int, _c_int, _c_dbl, _c_dbl,
+                                  _c_int, _c_int]),
     "unap_cuda_last_error": (ctypes.c_char_p, []),
     "unap_cuda_version": (ctypes.c_char_p, []),
     "unap_cuda_device_synchronize": (_c_int, []),
@@ -86,6 +110,7 @@ SIGNATURES = {
                                     ctypes.POINTER(_c_ll)]),
     "unap_cuda_amg_vcycle": (_c_int, [_c_long, _vp, _vp]),
     "unap_cuda_amg_eigenvalues": (_c_int, [_c_long, _vp, _c_int, _vp]),
+    "unap_cuda_amg_profile_smoother": (_c_int, [_c_long, _c_int, _c_int, _vp, _vp, _vp]),
     "unap_cuda_set_cheby_small_rows": (_c_int, [_c_int]),
     "unap_cuda_amg_profile_vcycle": (_c_int, [_c_long, _c_int, _vp, _c_int, _ip]),
     "unap_cuda_amg_solve": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
@@ -425,6 +450,14 @@ class DeviceAmg:
 
     def vcycle(self, r, z):
         check(load().unap_cuda_amg_vcycle(self.handle, _ptr(r), _ptr(z)))
+
+    def profile_smoother(self, level: int, reps: int = 10):
+        """(ms, algorithmic bytes, launches) of one smoothing launch group on
+        `level` (see unap_cuda_amg_profile_smoother)."""
+        ms, b, n = _c_dbl(), _c_dbl(), _c_int()
+        check(load().unap_cuda_amg_profile_smoother(self.handle, level, reps, ctypes.byref(ms),
+                                                    ctypes.byref(b), ctypes.byref(n)))
+        return ms.value, b.value, n.value
 
     def eigenvalues(self):
         """Chebyshev eigenvalue estimate of every level but the coarsest

@@ -657,6 +657,59 @@ void AmgHierarchy::vcycle(const Exec& ex, const double* r, double* z, Gate g)
     }
 }
 
+template <class T>
+static double time_smoother(AmgHierarchy& H, cudaStream_t s, int k, int reps, double* bytes,
+                            int* launches)
+{
+    const AmgHierarchy::Lv& V = H.lv[(size_t)k];
+    const Level& Lk = *V.L;
+    const Rows<T> R = rowsT<T>(Lk);
+    const bool fp32 = std::is_same<T, float>::value;
+    Exec ex{s, device_max_blocks()};
+    DevArray<T> x((size_t)V.n), t((size_t)V.n), b((size_t)V.n), w((size_t)V.n);
+    k_fill<T>(ex, V.n, x.p, T(0));
+    k_fill<T>(ex, V.n, t.p, T(0));
+    k_fill<T>(ex, V.n, b.p, T(1));
+    k_fill<T>(ex, V.n, w.p, T(0));
+    const bool cheb = H.isCheby(k);
+    auto run = [&]() {
+        if (cheb)
+            k_cheb_step<T>(ex, R, x.p, t.p, b.p, w.p, (T)V.d1[1 % H.params.chebyDegree],
+                           (T)V.d2[1 % H.params.chebyDegree], 0, Gate{});
+        else if (V.pack.rec.p && packed_sweeps() != 0 && R.wide)
+            gs_sweep_packed<T>(ex, Lk, V.pack, R.diag, x.p, b.p, false, false,
+                               packed_sweeps() == 3 ||
+                                   (packed_sweeps() == 1 && 2.0 * Lk.nf > 12.5 * Lk.n),
+                               Gate{});
+        else
+            gs_sweep<T>(ex, Lk, R, x.p, b.p, false, false, Gate{});
+    };
+    run();
+    cudaEvent_t e0, e1;
+    UNAP_CK(cudaEventCreate(&e0));
+    UNAP_CK(cudaEventCreate(&e1));
+    UNAP_CK(cudaEventRecord(e0, s));
+    for (int i = 0; i < reps; ++i) run();
+    UNAP_CK(cudaEventRecord(e1, s));
+    UNAP_CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    UNAP_CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (bytes)
+        *bytes = cheb ? cheb_bytes(V.n, Lk.nf, fp32, true) : sweep_bytes(V.n, V.n, Lk.nf, fp32);
+    if (launches) *launches = cheb ? 1 : Lk.nWave;
+    return (double)ms / std::max(reps, 1);
+}
+
+double AmgHierarchy::profileSmoother(cudaStream_t s, int k, int reps, double* bytes,
+                                     int* launches)
+{
+    if (k < 0 || k >= nLevels() - 1) throw std::invalid_argument("no smoothed level there");
+    return params.precision == 1 ? time_smoother<float>(*this, s, k, reps, bytes, launches)
+                                 : time_smoother<double>(*this, s, k, reps, bytes, launches);
+}
+
 int AmgHierarchy::profile(cudaStream_t s, int reps, double* ms, int maxOut)
 {
     const int nl = nLevels();

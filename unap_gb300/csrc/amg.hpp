@@ -69,6 +69,12 @@ public:
     // level k's own steps; a level running in the cluster tail holds the
     // whole tail's time and the levels below it 0); returns levels written
     int profile(cudaStream_t s, int reps, double* ms, int maxOut);
+    // mean time of one smoothing launch group on level k (< the coarsest)
+    // in the V-cycle's precision, over `reps` runs after one warm-up, on
+    // scratch vectors: a Chebyshev step (one launch) on Chebyshev levels, a
+    // forward Gauss-Seidel sweep (one launch per wavefront) otherwise.
+    // *bytes = its algorithmic bytes, *launches = launches per run.
+    double profileSmoother(cudaStream_t s, int k, int reps, double* bytes, int* launches);
     // the same V-cycle as a step program (mega.hpp); lv[0] is the finest
     void appendVcycle(std::vector<Step>& out, std::vector<LevelRows>& lv, const double* r,
                       double* z);

@@ -180,6 +180,17 @@ int unap_cuda_amg_profile_vcycle(long int amg, int reps, double* ms, int maxOut,
     });
 }
 
+int unap_cuda_amg_profile_smoother(long int amg, int level, int reps, double* ms, double* bytes,
+                                   int* launches)
+{
+    return guarded([&] {
+        AmgHandle* h = amg_from(amg);
+        if (reps < 1) throw std::invalid_argument("reps must be >= 1");
+        double t = h->H->profileSmoother(h->A->stream, level, reps, bytes, launches);
+        if (ms) *ms = t;
+    });
+}
+
 int unap_cuda_amg_eigenvalues(long int amg, double* lam, int maxOut, int* written)
 {
     return guarded([&] {

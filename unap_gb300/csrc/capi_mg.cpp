@@ -70,6 +70,28 @@ void fail(const char* where, int* nIter, double* res)
 
 }  // namespace
 
+namespace {
+
+void mg_solve_device(MgHandle* h, double* x, const double* b, unap_cuda_stats* stats)
+{
+    MgSolver& S = h->get();
+    S.params = h->p;
+    SolveStats st = S.solveDevice(x, b);
+    if (stats) {
+        stats->nIterations = st.nIter;
+        stats->converged = st.converged;
+        stats->singular = st.singular;
+        stats->status = st.status;
+        stats->initialResidual = st.initRes;
+        stats->finalResidual = st.finalRes;
+        stats->trueResidual = -1;
+        stats->seconds = st.seconds;
+        stats->algorithmicBytes = st.bytes;
+    }
+}
+
+}  // namespace
+
 extern "C" {
 
 void mgsolversolve_(double* x, long int* APtrPtr, double* b, int* nCells, int* aggl,
@@ -204,22 +226,39 @@ int unap_cuda_mg_levels(long int mg, int* nCoarseLevels, int* cells, int maxOut)
 
 int unap_cuda_mg_solve(long int mg, double* x, const double* b, unap_cuda_stats* stats)
 {
+    return guarded([&] { mg_solve_device(mg_from(mg), x, b, stats); });
+}
+
+int unap_cuda_mg_solve_host(long int mg, double* x, const double* b, unap_cuda_stats* stats)
+{
     return guarded([&] {
         MgHandle* h = mg_from(mg);
-        MgSolver& S = h->get();
-        S.params = h->p;
-        SolveStats st = S.solveDevice(x, b);
-        if (stats) {
-            stats->nIterations = st.nIter;
-            stats->converged = st.converged;
-            stats->singular = st.singular;
-            stats->status = st.status;
-            stats->initialResidual = st.initRes;
-            stats->finalResidual = st.finalRes;
-            stats->trueResidual = -1;
-            stats->seconds = st.seconds;
-            stats->algorithmicBytes = st.bytes;
-        }
+        if (!x || !b) throw std::invalid_argument("null vector");
+        const size_t n = (size_t)h->A->n();
+        DevArray<double> dx(n), db(n);
+        UNAP_CK(cudaMemcpyAsync(dx.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->A->stream));
+        UNAP_CK(cudaMemcpyAsync(db.p, b, n * sizeof(double), cudaMemcpyHostToDevice, h->A->stream));
+        mg_solve_device(h, dx.p, db.p, stats);
+        UNAP_CK(cudaMemcpyAsync(x, dx.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->A->stream));
+        UNAP_CK(cudaStreamSynchronize(h->A->stream));
+    });
+}
+
+int unap_cuda_mg_set(long int mg, int nPre, int nPost, int nFinest, int scaleCorr, double tol,
+                     double relTol, int maxIter, int minIter)
+{
+    return guarded([&] {
+        MgHandle* h = mg_from(mg);
+        if (nPre < 0 || nPost < 0 || nFinest < 0 || maxIter < 0 || minIter < 0)
+            throw std::invalid_argument("negative sweep or iteration count");
+        h->p.nPre = nPre;
+        h->p.nPost = nPost;
+        h->p.nFinest = nFinest;
+        h->p.scaleCorr = scaleCorr;
+        h->p.tol = tol;
+        h->p.relTol = relTol;
+        h->p.maxIter = maxIter;
+        h->p.minIter = minIter;
     });
 }
 

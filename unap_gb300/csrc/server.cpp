@@ -144,8 +144,14 @@ void Server::largeWorker()
             Method m = Method::PCG;
             bool flexible = false, restart = false;
             if (r->method == SERVE_AMG_MIXED || r->method == SERVE_AMG_FP64) {
+                // every level smoothed by Chebyshev steps of degree 3: no
+                // wavefront chains, which dominate small systems' V-cycles
                 AmgParams ap;
                 ap.precision = r->method == SERVE_AMG_MIXED ? 1 : 0;
+                ap.smoother = 1;
+                ap.chebyDegree = 3;
+                ap.chebyFrom = 0;
+                ap.eigRatio = 30.0;
                 H = std::make_unique<AmgHierarchy>(A, ap);
                 P = std::make_unique<AmgPrecond>(*H);
                 flexible = ap.precision == 1;

@@ -16,8 +16,8 @@
 namespace unapgpu {
 
 enum ServeMethod : int {
-    SERVE_AMG_MIXED = 0,  // AMG-PCG, FP32 V-cycle, flexible FP64 PCG
-    SERVE_AMG_FP64 = 1,   // AMG-PCG, FP64 V-cycle
+    SERVE_AMG_MIXED = 0,  // AMG-PCG, FP32 Chebyshev V-cycle, flexible FP64 PCG
+    SERVE_AMG_FP64 = 1,   // AMG-PCG, FP64 Chebyshev V-cycle
     SERVE_PCG_DIC = 2,    // PCG + DIC
     SERVE_BICG_DILU = 3,  // PBiCGStab + DILU
 };

@@ -64,24 +64,17 @@ class LduSystem:
 
 def grid_faces(nx: int, ny: int, nz: int) -> tuple[np.ndarray, np.ndarray]:
     """Face list (a, b) of an nx*ny*nz hex grid in natural cell order
-    c = i + nx*(j + ny*k); faces come out sorted by (owner, neighbour)."""
-    idx = np.arange(nx * ny * nz, dtype=np.int64).reshape(nz, ny, nx)
-    parts_a, parts_b = [], []
-    if nx > 1:
-        parts_a.append(idx[:, :, :-1])
-        parts_b.append(idx[:, :, 1:])
-    if ny > 1:
-        parts_a.append(idx[:, :-1, :])
-        parts_b.append(idx[:, 1:, :])
-    if nz > 1:
-        parts_a.append(idx[:-1, :, :])
-        parts_b.append(idx[1:, :, :])
-    if not parts_a:
-        return np.zeros(0, np.int64), np.zeros(0, np.int64)
-    a = np.concatenate([p.ravel() for p in parts_a])
-    b = np.concatenate([p.ravel() for p in parts_b])
-    order = np.lexsort((b, a))
-    return a[order], b[order]
+    c = i + nx*(j + ny*k); faces come out sorted by (owner, neighbour): each
+    cell's +x, +y, +z faces, cells in order."""
+    n = nx * ny * nz
+    c = np.arange(n, dtype=np.int64)
+    i = c % nx
+    j = (c // nx) % ny
+    k = c // (nx * ny)
+    nb = np.stack([c + 1, c + nx, c + nx * ny], axis=1)
+    ok = np.stack([i < nx - 1, j < ny - 1, k < nz - 1], axis=1)
+    a = np.broadcast_to(c[:, None], nb.shape)[ok]
+    return a, nb[ok]
 
 
 def _orient_and_sort(n: int, a: np.ndarray, b: np.ndarray, perm: np.ndarray | None,
@@ -95,7 +88,9 @@ def _orient_and_sort(n: int, a: np.ndarray, b: np.ndarray, perm: np.ndarray | No
     l = np.minimum(a, b)
     u = np.maximum(a, b)
     flip = a > b
-    order = np.lexsort((u, l))
+    # (l, u) pairs are unique, so one sort of the combined key gives the
+    # lexicographic order
+    order = np.argsort(l.astype(np.int64) * max(n, 1) + u)
     out = [l[order].astype(np.int32), u[order].astype(np.int32), flip[order]]
     out += [d[order] for d in face_data]
     return out
@@ -200,33 +195,58 @@ def grid_for(cells: int, rng) -> tuple[int, int, int]:
     return int(dims[0]), int(dims[1]), int(dims[2])
 
 
-def serving_requests(count: int = 2000, rate: float = 200.0, min_cells: int = 8_000,
-                     max_cells: int = 2_000_000, seed: int = 0) -> list[Request]:
-    """The serving stream (config c5): Poisson arrivals at `rate` per second,
-    sizes log-uniform in [min_cells, max_cells], permuted LDU on cubic or
-    elongated grids; 60% log-normal Poisson solved by mixed AMG-PCG, 25%
-    Laplacian by PCG+DIC, 15% convection-diffusion (Pe ~ U[1, 10]) by
-    PBiCGStab+DILU."""
+@dataclasses.dataclass
+class RequestSpec:
+    """One request of the serving stream before its matrix is built."""
+    arrival: float
+    dims: tuple[int, int, int]
+    method: str
+    seed: int
+    pe: float = 0.0
+
+
+def serving_stream(count: int = 2000, rate: float = 200.0, min_cells: int = 8_000,
+                   max_cells: int = 2_000_000, seed: int = 0) -> list[RequestSpec]:
+    """The serving stream (config c5) as request specifications: Poisson
+    arrivals at `rate` per second, sizes log-uniform in [min_cells,
+    max_cells] on cubic or elongated grids; 60% log-normal Poisson (mixed
+    AMG-PCG), 25% Laplacian (PCG+DIC), 15% convection-diffusion with
+    Pe ~ U[1, 10] (PBiCGStab+DILU).  `build_request` makes the matrix."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
-    for i in range(count):
+    for _ in range(count):
         t += rng.exponential(1.0 / rate)
         cells = float(np.exp(rng.uniform(np.log(min_cells), np.log(max_cells))))
-        nx, ny, nz = grid_for(int(cells), rng)
+        dims = grid_for(int(cells), rng)
         u = rng.random()
         s_seed = int(rng.integers(1 << 31))
         if u < 0.60:
-            s = lognormal(nx, ny, nz, seed=s_seed, permute=True, sigma=2.0)
-            method = "amg_mixed"
+            out.append(RequestSpec(t, dims, "amg_mixed", s_seed))
         elif u < 0.85:
-            s = laplace(nx, ny, nz, seed=s_seed, permute=True, rhs="uniform")
-            method = "pcg_dic"
+            out.append(RequestSpec(t, dims, "pcg_dic", s_seed))
         else:
-            s = convdiff(nx, ny, nz, seed=s_seed, permute=True, pe=float(rng.uniform(1, 10)))
-            method = "bicgstab_dilu"
-        out.append(Request(t, s, method, s_seed))
+            out.append(RequestSpec(t, dims, "bicgstab_dilu", s_seed, float(rng.uniform(1, 10))))
     return out
+
+
+def build_request(spec: RequestSpec) -> Request:
+    """The permuted LDU system of one stream request."""
+    nx, ny, nz = spec.dims
+    if spec.method == "amg_mixed":
+        s = lognormal(nx, ny, nz, seed=spec.seed, permute=True, sigma=2.0)
+    elif spec.method == "pcg_dic":
+        s = laplace(nx, ny, nz, seed=spec.seed, permute=True, rhs="uniform")
+    else:
+        s = convdiff(nx, ny, nz, seed=spec.seed, permute=True, pe=spec.pe)
+    return Request(spec.arrival, s, spec.method, spec.seed)
+
+
+def serving_requests(count: int = 2000, rate: float = 200.0, min_cells: int = 8_000,
+                     max_cells: int = 2_000_000, seed: int = 0) -> list[Request]:
+    """The serving stream (config c5) with every matrix built (see
+    serving_stream)."""
+    return [build_request(sp) for sp in serving_stream(count, rate, min_cells, max_cells, seed)]
 
 
 def config(name: str, scale: float = 1.0, seed: int = 0) -> LduSystem:
