@@ -577,6 +577,31 @@ def kernels_case(args):
     A.close()
 
 
+def smoother_case(args):
+    """One smoothing launch group (a Chebyshev step, or a Gauss-Seidel sweep)
+    on AMG level `--smoother-level` of the workload's hierarchy, timed with
+    CUDA events after one warm-up (the small case for kernel profiles)."""
+    import torch
+    from unap_gb300 import capi
+    from unap_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    wl = WORKLOADS[args.workload]
+    s = W.config(args.workload, args.scale, seed=0)
+    A = capi.DeviceMatrix(s)
+    G = capi.DeviceAmg(A, precision=wl["precision"], rel_tol=wl["rel_tol"], n_coarsest=1000,
+                       **amg_kwargs(wl))
+    sizes = G.level_sizes()
+    k = args.smoother_level
+    ms, by, launches = G.profile_smoother(k, reps=args.reps)
+    print(json.dumps({"workload": args.workload, "scale": args.scale, "level": k,
+                      "rows": sizes[k][0], "faces": sizes[k][1], "ms": ms,
+                      "algorithmic_bytes": by, "launches": launches,
+                      "achieved_gbs": by / (ms * 1e-3) / 1e9}), flush=True)
+    G.close()
+    A.close()
+
+
 def textio_case(args):
     """Host text I/O of the workload's matrix in the reference's LDU dump
     format: print it, read it back (both through the C ABI, from a pool of
@@ -744,6 +769,9 @@ def main():
                     help="bracket one extra mixed solve after the timed ones (with --setup: "
                          "the device setup) with cudaProfilerStart/Stop, for ncu "
                          "--profile-from-start off")
+    ap.add_argument("--smoother-level", type=int, default=-1,
+                    help="only time one smoothing launch group on this AMG level (the small "
+                         "case for kernel profiles) and exit")
     ap.add_argument("--setup", action="store_true",
                     help="only time the matrix and hierarchy setup, device vs host, and exit")
     ap.add_argument("--textio", action="store_true",
@@ -759,6 +787,9 @@ def main():
         raise SystemExit("--warmup must be >= 3")
     if args.kernels:
         kernels_case(args)
+        return
+    if args.smoother_level >= 0:
+        smoother_case(args)
         return
     world, rank, local, dist = dist_setup(args)
     if args.impl == "reference":

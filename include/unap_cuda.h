@@ -209,10 +209,12 @@ int unap_cuda_spmv(long int handle, const double* x, double* y);
  * its scratch is a static device array of 2 x 1,048,576 doubles (16 MiB,
  * held by every GPU that loads the library until exit), so matrices above
  * 1,048,576 cells are rejected (UNAP_CUDA_EINVAL).  The handle must already
- * be built on the device.  The first call on a device looks up the array's
- * device address; make it before any stream capture begins.  All calls share
- * the array: calls whose work overlaps on the GPU race; calls on one stream
- * are safe. */
+ * be built on the device.  The call runs on the device the matrix was built
+ * on (whichever device is current) and is synchronous: it returns when its
+ * kernels have finished, so it must not be called while a stream capture is
+ * active on the calling thread.  Its first call on a device looks up the
+ * array's device address.  All calls share the array: calls whose work
+ * overlaps on the GPU race; calls on one stream are safe. */
 int unap_cuda_spmv_noalloc(long int handle, const double* x, double* y);
 /* w = M^-1 r, precond 1 Diag, 2 DIC, 3 DILU */
 int unap_cuda_precondition(long int handle, int precond, const double* r, double* w);
@@ -464,6 +466,13 @@ int unap_cuda_set_packed_sweeps(int mode);
  * CTAs would be (default 100000).  Results are identical.  Returns the
  * previous setting.  No counterpart in the reference. */
 int unap_cuda_set_cheby_small_rows(int rows);
+/* Entries of a row the Chebyshev step loads per dependent round trip: 0
+ * (default) 16 on levels averaging more than 8 entries per row and 8
+ * elsewhere, or 8 / 16 everywhere (fewer registers and more resident warps
+ * against one round trip per row).  Results are identical.  Returns the
+ * previous setting, or UNAP_CUDA_EINVAL for another value.  No counterpart
+ * in the reference. */
+int unap_cuda_set_cheby_chunk(int entries);
 
 /* Coarse-level tail of the AMG V-cycle (per-step executor), set for the FP64
  * (precision 0) or FP32 (precision 1) V-cycle: every level with at most

@@ -84,22 +84,28 @@ def test_cheby_eigenvalues_and_vcycle_bit_exact(cuda, orc, precision, case):
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_cheby_launch_geometry_same_bits(cuda, precision):
-    """One-warp or 256-thread CTAs for the Chebyshev steps: same bits."""
+    """One-warp or 256-thread CTAs and 8- or 16-entry load chunks for the
+    Chebyshev steps: same bits."""
     torch = cuda
     s = W.lognormal(24, 20, 18, seed=11, permute=True)
     A = capi.DeviceMatrix(s)
     G = capi.DeviceAmg(A, n_coarsest=60, precision=precision, smoother=1)
     r = dev(torch, np.random.default_rng(3).standard_normal(s.n))
     out = []
-    for rows in (0, 1 << 30):
+    for rows, chunk in ((0, 0), (1 << 30, 0), (0, 8), (1 << 30, 16)):
         old = capi.set_cheby_small_rows(rows)
+        oldc = capi.set_cheby_chunk(chunk)
         try:
             z = torch.zeros(s.n, dtype=torch.float64, device="cuda")
             G.vcycle(r, z)
             out.append(z.cpu().numpy())
         finally:
             capi.set_cheby_small_rows(old)
-    assert np.array_equal(out[0], out[1])
+            capi.set_cheby_chunk(oldc)
+    for o in out[1:]:
+        assert np.array_equal(out[0], o)
+    with pytest.raises(capi.UnapCudaError):
+        capi.set_cheby_chunk(5)
     G.close()
     A.close()
 

@@ -9,7 +9,7 @@ same iteration count and the same solution bits from the device and host
 structure builds, and mixed precision agreeing with FP64.
 
 c1  32^3 natural-order Laplacian, PCG+DIC, tol 1e-8 (also solved by the oracle)
-c2  128^3 permuted Laplacian, FP64 AMG-PCG, tol 1e-10
+c2  128^3 permuted Laplacian, FP64 AMG-PCG, tol 1e-10 (also solved by the oracle)
 c3  200^3 permuted convection-diffusion Pe=5, PBiCGStab+DILU, tol 1e-9
 c4  256^3 permuted log-normal (sigma 2) Poisson, mixed vs FP64 AMG-PCG, tol 1e-10
 """
@@ -63,11 +63,28 @@ def test_c2_full(cuda, orc):
     z = torch.zeros(s.n, dtype=torch.float64, device="cuda")
     G.vcycle(dev(torch, v), z)
     assert np.array_equal(z.cpu().numpy(), O.vcycle(v))
-    O.close()
     x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
     st = G.solve(x, dev(torch, s.b))
     assert st["converged"]
-    assert true_rel(orc, s, x.cpu().numpy()) <= 1.0001e-10
+    xg = x.cpu().numpy()
+    assert true_rel(orc, s, xg) <= 1.0001e-10
+    # the oracle's own FP64 AMG-PCG at full size: the same iteration count
+    # +-1 and agreement in residual space at relTol 1e-10, and solutions
+    # within 1e-10 relative 2-norm at relTol 1e-13
+    x_ref, st_ref = O.solve(s.b)
+    assert st_ref["converged"] and abs(st["nIterations"] - st_ref["n_iter"]) <= 1, (st, st_ref)
+    assert np.linalg.norm(orc.spmv(s, xg - x_ref)) <= 2.2e-10 * st_ref["init_res"]
+    O.close()
+    G.close()
+    G = capi.DeviceAmg(A, n_coarsest=1000, precision=0, rel_tol=1e-13)
+    O = OracleAmg(orc, s, n_coarsest=1000, precision=0, rel_tol=1e-13)
+    x.zero_()
+    st = G.solve(x, dev(torch, s.b))
+    x_ref, st_ref = O.solve(s.b)
+    assert abs(st["nIterations"] - st_ref["n_iter"]) <= 1, (st, st_ref)
+    xg = x.cpu().numpy()
+    assert np.linalg.norm(xg - x_ref) <= 1e-10 * np.linalg.norm(x_ref)
+    O.close()
     G.close()
     A.close()
 

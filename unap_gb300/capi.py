@@ -112,6 +112,7 @@ SIGNATURES = {
     "unap_cuda_amg_eigenvalues": (_c_int, [_c_long, _vp, _c_int, _vp]),
     "unap_cuda_amg_profile_smoother": (_c_int, [_c_long, _c_int, _c_int, _vp, _vp, _vp]),
     "unap_cuda_set_cheby_small_rows": (_c_int, [_c_int]),
+    "unap_cuda_set_cheby_chunk": (_c_int, [_c_int]),
     "unap_cuda_amg_profile_vcycle": (_c_int, [_c_long, _c_int, _vp, _c_int, _ip]),
     "unap_cuda_amg_solve": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
     "unap_cuda_amg_solve_host": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
@@ -325,6 +326,15 @@ def set_cheby_small_rows(rows: int) -> int:
     """Chebyshev-step launches on levels of at most `rows` rows use one-warp
     CTAs; returns the previous threshold."""
     return int(load().unap_cuda_set_cheby_small_rows(int(rows)))
+
+
+def set_cheby_chunk(entries: int) -> int:
+    """Entries per load round trip of the Chebyshev step (0 auto, 8, 16);
+    returns the previous value."""
+    rc = int(load().unap_cuda_set_cheby_chunk(int(entries)))
+    if rc < 0:
+        check(rc)
+    return rc
 
 
 def set_tail_rows(tail_rows: int, single_rows: int, precision: int | None = None):

@@ -58,13 +58,15 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
         CoarseHost& c = coarse[(size_t)k - 1];
         const Level& F = *lv[(size_t)k - 1].L;
         const int nC = c.A.n;
-        // locality key of a coarse cell: first internal position of its cells
+        // locality key of a coarse cell: the first locality rank of its
+        // cells on the finer level (BFS order on the finest)
         std::vector<int> key((size_t)nC, INT_MAX);
         for (int i = 0; i < F.n; ++i) {
             int C = c.restrictAddr[(size_t)i];
-            key[(size_t)C] = std::min(key[(size_t)C], F.iperm[(size_t)i]);
+            key[(size_t)C] = std::min(key[(size_t)C], F.locRank[(size_t)i]);
         }
-        lv[(size_t)k].own = build_level(c.A, &key, k == L, s);
+        // Chebyshev levels are never swept: locality order, no wavefronts
+        lv[(size_t)k].own = build_level(c.A, &key, k == L, s, !isCheby(k));
         lv[(size_t)k].L = lv[(size_t)k].own.get();
         lv[(size_t)k].n = nC;
         const Level& Cl = *lv[(size_t)k].L;
@@ -156,7 +158,7 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
     // row-packed copies of the levels the cluster tail may run (in the
     // precision of the V-cycle)
     for (int k = 0; k < L; ++k) {
-        if (lv[(size_t)k].n > kTailPackRows) continue;
+        if (lv[(size_t)k].n > kTailPackRows || isCheby(k)) continue;
         if (params.precision == 1)
             pack_rows<float>(rows32(*lv[(size_t)k].L), lv[(size_t)k].pack, s);
         else
@@ -268,12 +270,10 @@ void AmgHierarchy::setupCheby(cudaStream_t s)
         UNAP_CK(cudaMemcpyAsync(es.p, &h, sizeof(EigState), cudaMemcpyHostToDevice, s));
         eig_diag_pcg(ex, rows64(Lk), rD.p, x.p, b.p, rA.p, wA.p, pA.p, es.p,
                      pool.site(0, nullptr, FIN_RES_ONLY), pool.site(1, nullptr, FIN_RES_ONLY), 10);
+        k_eig_sturm(ex, es.p, 10);
         UNAP_CK(cudaMemcpyAsync(&h, es.p, sizeof(EigState), cudaMemcpyDeviceToHost, s));
         UNAP_CK(cudaStreamSynchronize(s));
-        int nP = 0;
-        while (nP < 10 && h.alphas[nP] != 0.0) ++nP;
-        V.lam = nP >= 2 ? lanczos_max_eig(h.alphas, h.betas, nP)
-                        : (nP == 1 ? 1.0 / h.alphas[0] : 1.0);
+        V.lam = h.maxEig;
         cheby_coeffs(V.lam, params.eigRatio, params.chebyDegree, &V.Rth, V.d1, V.d2);
         if (params.precision == 1)
             V.tf.alloc((size_t)n);

@@ -245,6 +245,16 @@ int unap_cuda_set_packed_sweeps(int mode) { return set_packed_sweeps(mode); }
 
 int unap_cuda_set_cheby_small_rows(int rows) { return set_cheby_small_rows(rows); }
 
+int unap_cuda_set_cheby_chunk(int entries)
+{
+    try {
+        return set_cheby_chunk(entries);
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return UNAP_CUDA_EINVAL;
+    }
+}
+
 int unap_cuda_set_tail_rows(int precision, long long tailRows, long long singleRows,
                             long long* oldTailRows, long long* oldSingleRows)
 {

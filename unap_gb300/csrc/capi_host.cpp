@@ -314,12 +314,10 @@ int unap_cuda_cheby_smooth_host(long int handle, double* x, const double* b, int
             eig_diag_pcg(ex, R, rD.p, xi.p, bi.p, t.p, w.p, pA.p, es.p,
                          pool.site(0, nullptr, FIN_RES_ONLY), pool.site(1, nullptr, FIN_RES_ONLY),
                          10);
+            k_eig_sturm(ex, es.p, 10);
             UNAP_CK(cudaMemcpyAsync(&st, es.p, sizeof st, cudaMemcpyDeviceToHost, A.stream));
             UNAP_CK(cudaStreamSynchronize(A.stream));
-            int nP = 0;
-            while (nP < 10 && st.alphas[nP] != 0.0) ++nP;
-            *maxEig = nP >= 2 ? lanczos_max_eig(st.alphas, st.betas, nP)
-                              : (nP == 1 ? 1.0 / st.alphas[0] : 0.0);
+            *maxEig = st.maxEig;
             *estimated = 1;
         } else if (nSweeps > 0) {
             // chebySmoother.cpp:44-148 on [maxEig / 1.5, 1.1 maxEig]

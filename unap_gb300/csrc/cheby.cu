@@ -17,6 +17,7 @@ void tick()
 }
 
 std::atomic<int> g_smallRows{100000};
+std::atomic<int> g_chunk{0};  // 0: 16 entries on long-row levels, else 8
 
 // ---- eigenDiagPCG::diagPCGLoops (eigenDiagPCG.cpp:48-238) ----------------
 __global__ void __launch_bounds__(kBlock) eig_wr_kernel(int n, const double* __restrict__ rD,
@@ -83,6 +84,58 @@ __global__ void eig_update_kernel(int n, double* __restrict__ x, double* __restr
         x[i] += alpha * pA[i];
         rA[i] -= alpha * wA[i];
     }
+}
+
+// Lanczos tridiagonal + Sturm-sequence bisection to 1e-5 (k = 1), over the
+// iterations the diagonal PCG completed
+__global__ void eig_sturm_kernel(EigState* es, int nMax)
+{
+    int nP = 0;
+    while (nP < nMax && nP < 16 && es->alphas[nP] != 0.0) ++nP;
+    if (nP < 2) {
+        es->maxEig = nP == 1 ? 1.0 / es->alphas[0] : 1.0;
+        return;
+    }
+    double T[16][16];
+    for (int i = 0; i < nP; ++i)
+        for (int j = 0; j < nP; ++j) T[i][j] = 0;
+    for (int i = 0; i < nP; ++i) {
+        if (i == 0)
+            T[i][i] = 1.0 / es->alphas[i];
+        else
+            T[i][i] = 1.0 / es->alphas[i] + es->betas[i] / es->alphas[i - 1];
+        if (i < nP - 1) T[i][i + 1] = sqrt(es->betas[i + 1]) / es->alphas[i];
+        if (i > 0) T[i][i - 1] = T[i - 1][i];
+    }
+    double xBegin = 0.0, xEnd = 0.0;
+    for (int i = 0; i < nP; ++i) {
+        double Tr = (i == nP - 1) ? 0 : T[i][i + 1];
+        double Tl = (i == 0) ? 0 : T[i][i - 1];
+        double lambMax = T[i][i] + fabs(Tr) + fabs(Tl);
+        double lambMin = T[i][i] - fabs(Tr) - fabs(Tl);
+        xBegin = (xBegin >= lambMin) ? lambMin : xBegin;
+        xEnd = (xEnd <= lambMax) ? lambMax : xEnd;
+    }
+    double p[16];
+    double xn = 0.0;
+    int guard = 0;
+    do {
+        xn = (xBegin + xEnd) * 0.5;
+        int s = 0;
+        p[0] = xn - T[0][0];
+        if (p[0] < 0) s = 1;
+        p[1] = (xn - T[1][1]) * p[0] - T[0][1] * T[0][1];
+        if (p[1] * p[0] < 0) s++;
+        for (int k = 2; k < nP; ++k) {
+            p[k] = (xn - T[k][k]) * p[k - 1] - T[k - 1][k] * T[k - 1][k] * p[k - 2];
+            if (p[k] * p[k - 1] < 0) s++;
+        }
+        if (s >= 1)
+            xBegin = xn;
+        else
+            xEnd = xn;
+    } while ((xEnd - xBegin) >= 0.00001 && ++guard < 4096);
+    es->maxEig = xn;
 }
 
 // splitmix64 (Steele, Lea and Flood, 2014): the eigenvalue start vector
@@ -221,6 +274,13 @@ __global__ void prolong_to_kernel(int n, const int* __restrict__ cmap, const T* 
 
 int set_cheby_small_rows(int rows) { return g_smallRows.exchange(rows); }
 
+int set_cheby_chunk(int entries)
+{
+    if (entries != 0 && entries != 8 && entries != 16)
+        throw std::invalid_argument("Chebyshev chunk must be 0, 8 or 16 entries");
+    return g_chunk.exchange(entries);
+}
+
 void eig_diag_pcg(const Exec& ex, const Rows<double>& A, const double* rD, double* x,
                   const double* b, double* rA, double* wA, double* pA, EigState* es,
                   const RSpec& wr, const RSpec& al, int nIt)
@@ -240,46 +300,11 @@ void eig_diag_pcg(const Exec& ex, const Rows<double>& A, const double* rD, doubl
     UNAP_CK(cudaGetLastError());
 }
 
-double lanczos_max_eig(const double* alphas, const double* betas, int nP)
+void k_eig_sturm(const Exec& ex, EigState* es, int nMax)
 {
-    std::vector<double> T((size_t)nP * nP, 0.0), p((size_t)nP, 0.0);
-    auto t = [&](int i, int j) -> double& { return T[(size_t)i * nP + j]; };
-    for (int i = 0; i < nP; ++i) {
-        if (i == 0)
-            t(i, i) = 1.0 / alphas[i];
-        else
-            t(i, i) = 1.0 / alphas[i] + betas[i] / alphas[i - 1];
-        if (i < nP - 1) t(i, i + 1) = std::sqrt(betas[i + 1]) / alphas[i];
-        if (i > 0) t(i, i - 1) = t(i - 1, i);
-    }
-    double xBegin = 0.0, xEnd = 0.0;
-    for (int i = 0; i < nP; ++i) {
-        const double Tr = (i == nP - 1) ? 0 : t(i, i + 1);
-        const double Tl = (i == 0) ? 0 : t(i, i - 1);
-        const double lambMax = t(i, i) + std::fabs(Tr) + std::fabs(Tl);
-        const double lambMin = t(i, i) - std::fabs(Tr) - std::fabs(Tl);
-        xBegin = (xBegin >= lambMin) ? lambMin : xBegin;
-        xEnd = (xEnd <= lambMax) ? lambMax : xEnd;
-    }
-    double xn = 0.0;
-    int guard = 0;
-    do {
-        xn = (xBegin + xEnd) * 0.5;
-        int s = 0;
-        p[0] = xn - t(0, 0);
-        if (p[0] < 0) s = 1;
-        p[1] = (xn - t(1, 1)) * p[0] - std::pow(t(0, 1), 2.0);
-        if (p[1] * p[0] < 0) s++;
-        for (int k = 2; k < nP; ++k) {
-            p[(size_t)k] = (xn - t(k, k)) * p[(size_t)k - 1] - std::pow(t(k - 1, k), 2.0) * p[(size_t)k - 2];
-            if (p[(size_t)k] * p[(size_t)k - 1] < 0) s++;
-        }
-        if (s >= 1)
-            xBegin = xn;
-        else
-            xEnd = xn;
-    } while ((xEnd - xBegin) >= 0.00001 && ++guard < 4096);
-    return xn;
+    tick();
+    eig_sturm_kernel<<<1, 1, 0, ex.s>>>(es, nMax);
+    UNAP_CK(cudaGetLastError());
 }
 
 void k_eig_start(const Exec& ex, int n, const int* perm, double* b)
@@ -332,7 +357,8 @@ void k_cheb_step(const Exec& ex, const Rows<T>& A, const T* xin, T* xout, const 
     cfg.attrs = at;
     cfg.numAttrs = wave_pdl() ? 1 : 0;
     tick();
-    if (A.wide)
+    const int ck = g_chunk.load();
+    if (ck == 16 || (ck == 0 && A.wide))
         UNAP_CK(cudaLaunchKernelEx(&cfg, cheb_step_kernel<T, 16>, A, xin, xout, b, w, c1, c2,
                                    first, g));
     else

@@ -34,10 +34,11 @@ void eig_diag_pcg(const Exec& ex, const Rows<double>& A, const double* rD, doubl
                   const double* b, double* rA, double* wA, double* pA, EigState* es,
                   const RSpec& wr, const RSpec& al, int nIt);
 
-// eigenDiagPCG::computeMaxEig (eigenDiagPCG.cpp:242-361) on the host: the
-// Lanczos tridiagonal of nP >= 2 iterations, Sturm-sequence bisection to a
-// band of 1e-5.
-double lanczos_max_eig(const double* alphas, const double* betas, int nP);
+// eigenDiagPCG::computeMaxEig (eigenDiagPCG.cpp:242-361) on one device
+// thread: es->maxEig = the largest eigenvalue of the Lanczos tridiagonal of
+// the iterations done (nonzero alphas, at most nMax <= 16) by Sturm-sequence
+// bisection to a band of 1e-5; 1 / alpha_0 after one iteration, 1 after none.
+void k_eig_sturm(const Exec& ex, EigState* es, int nMax);
 
 // Start vector of the AMG levels' eigenvalue estimate: cell c (reference
 // numbering of its level) gets a uniform value in [-1, 1) from splitmix64.
@@ -76,5 +77,9 @@ void k_prolong_add_to(const Exec& ex, int n, const int* cmap, const T* coarse, c
 // Rows per level below which Chebyshev-step launches use one-warp CTAs
 // (spread over more SMs); returns the previous value.
 int set_cheby_small_rows(int rows);
+// Entries of a row loaded per dependent round trip by the Chebyshev step: 0
+// (default) 16 on levels averaging more than 8 entries per row, else 8; 8 or
+// 16 on every level.  Returns the previous value.
+int set_cheby_chunk(int entries);
 
 }  // namespace unapgpu

@@ -30,6 +30,7 @@ const char* last_error() { return g_last_error.c_str(); }
 // ---- Matrix ----------------------------------------------------------------
 Matrix::Matrix(HostLdu&& h, cudaStream_t s) : host(std::move(h)), stream(s)
 {
+    UNAP_CK(cudaGetDevice(&device));
     if (!stream) {
         UNAP_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         ownsStream = true;

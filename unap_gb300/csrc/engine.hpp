@@ -27,6 +27,7 @@ public:
     std::unique_ptr<Level> L;
     cudaStream_t stream;
     bool ownsStream = false;
+    int device = 0;  // the GPU the matrix was built on (current at construction)
     int n() const { return host.n; }
     // replace the coefficients (same addressing)
     void setValues(const double* diag, const double* upper, const double* lower);

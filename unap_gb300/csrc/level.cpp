@@ -82,12 +82,12 @@ std::vector<int> bfs_rank(int n, const std::vector<int>& loStart, const std::vec
 }  // namespace
 
 std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key,
-                                   bool identityOrder, cudaStream_t s)
+                                   bool identityOrder, cudaStream_t s, bool wavefronts)
 {
     const long long minCells = device_setup_min_cells();
     if (!identityOrder && A.oriented && A.ownerSorted && minCells >= 0 && A.n > 0 &&
         A.n >= minCells) {
-        if (auto D = build_level_device(A, key, s)) {
+        if (auto D = build_level_device(A, key, s, wavefronts)) {
             D->version = next_version();
             return D;
         }
@@ -98,7 +98,7 @@ std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key
     L->n = n;
     L->nf = nf;
     L->symm = A.symm;
-    L->sweepable = A.oriented && A.ownerSorted;
+    L->sweepable = A.oriented && A.ownerSorted && (wavefronts || identityOrder);
     const int* l = A.l.data();
     const int* u = A.u.data();
 
@@ -109,7 +109,7 @@ std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key
     // forward wavefront of every cell: 1 + max over lower neighbours
     std::vector<int> wave((size_t)n, 0);
     int nWave = 1;
-    if (L->sweepable && !identityOrder) {
+    if (L->sweepable && !identityOrder && wavefronts) {
         for (int c = 0; c < n; ++c) {
             int w = 0;
             for (int k = loStart[(size_t)c]; k < loStart[(size_t)c + 1]; ++k) {
@@ -130,8 +130,10 @@ std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key
     // internal order: wavefront-major, locality key inside a wavefront
     L->perm.resize((size_t)n);
     L->iperm.resize((size_t)n);
+    L->locRank.resize((size_t)n);
     if (identityOrder) {
         std::iota(L->perm.begin(), L->perm.end(), 0);
+        std::iota(L->locRank.begin(), L->locRank.end(), 0);
         L->waveStart = {0, n};
         L->nWave = n ? 1 : 0;
     } else {
@@ -154,6 +156,7 @@ std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key
             for (int k = 0; k <= maxKey; ++k) cnt[(size_t)k + 1] += cnt[(size_t)k];
             for (int c = 0; c < n; ++c) byKey[(size_t)cnt[(size_t)rank[(size_t)c]]++] = c;
         }
+        for (int i = 0; i < n; ++i) L->locRank[(size_t)byKey[(size_t)i]] = i;
         L->waveStart.assign((size_t)nWave + 1, 0);
         for (int c = 0; c < n; ++c) L->waveStart[(size_t)wave[(size_t)c] + 1]++;
         for (int w = 0; w < nWave; ++w) L->waveStart[(size_t)w + 1] += L->waveStart[(size_t)w];

@@ -550,7 +550,7 @@ long long device_setup_min_cells() { return g_deviceMinCells.load(); }
 // than kMaxWaves wavefronts or kMaxComponents connected components, or a
 // locality key that repeats; build_level then builds it on the host.
 std::unique_ptr<Level> build_level_device(const HostLdu& A, const std::vector<int>* key,
-                                          cudaStream_t s)
+                                          cudaStream_t s, bool wavefronts)
 {
     const int n = A.n, nf = A.nf;
     if (n <= 0) return nullptr;
@@ -593,7 +593,11 @@ std::unique_ptr<Level> build_level_device(const HostLdu& A, const std::vector<in
     // 3: forward wavefronts
     Scratch<int> wave((size_t)n, s), indeg((size_t)n, s), fa((size_t)n, s), fb((size_t)n, s);
     int nWave = 0;
-    {
+    if (!wavefronts) {
+        // one range: every row in locality order
+        UNAP_CK(cudaMemsetAsync(wave.p, 0, sizeof(int) * (size_t)n, s));
+        nWave = 1;
+    } else {
         UNAP_CK(cudaMemsetAsync(flags.p, 0, sizeof(int), s));
         k_wave_init<<<grid_for(n), kThreads, 0, s>>>(loStart.p, n, indeg.p, wave.p, fa.p, flags.p);
         int m = rb.get(flags.p);
@@ -683,7 +687,7 @@ std::unique_ptr<Level> build_level_device(const HostLdu& A, const std::vector<in
     L->n = n;
     L->nf = nf;
     L->symm = A.symm;
-    L->sweepable = true;
+    L->sweepable = wavefronts;
     L->nWave = nWave;
     L->d_perm.alloc((size_t)n);
     L->d_iperm.alloc((size_t)n);
@@ -699,6 +703,8 @@ std::unique_ptr<Level> build_level_device(const HostLdu& A, const std::vector<in
         k_split<true><<<warpsGrid, kThreads, 0, s>>>(byKey.p, wave.p, n, nWave, cnt.p, ws.p, L->d_perm.p);
     }
     k_iperm<<<grid_for(n), kThreads, 0, s>>>(L->d_perm.p, n, L->d_iperm.p);
+    Scratch<int> locRank((size_t)n, s);
+    k_iperm<<<grid_for(n), kThreads, 0, s>>>(byKey.p, n, locRank.p);
     UNAP_CK(cudaGetLastError());
 
     // 6: SELL-32
@@ -757,6 +763,7 @@ std::unique_ptr<Level> build_level_device(const HostLdu& A, const std::vector<in
     // host copies the rest of the library reads
     to_host(L->perm, L->d_perm.p, (size_t)n, s);
     to_host(L->iperm, L->d_iperm.p, (size_t)n, s);
+    to_host(L->locRank, locRank.p, (size_t)n, s);
     to_host(L->waveStart, ws.p, (size_t)nWave + 1, s);
     to_host(L->entLo, entLo.p, (size_t)nf, s);
     to_host(L->entUp, entUp.p, (size_t)nf, s);

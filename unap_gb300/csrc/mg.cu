@@ -63,53 +63,6 @@ __global__ void __launch_bounds__(kBlock) scaling_kernel(int n, const double* __
     reduce_launch<2>(v, red, [&](const double (&t)[2]) { *sfOut = t[0] / (t[1] + SMALL_D); });
 }
 
-// ---- eigenDiagPCG (eigenDiagPCG.cpp:242-361); the diagonal-PCG loops are
-// eig_diag_pcg (cheby.cu) --------------------------------------------------
-// Lanczos tridiagonal + Sturm-sequence bisection to 1e-5 (k = 1)
-__global__ void eig_sturm_kernel(EigState* es, int nP)
-{
-    double T[16][16];
-    for (int i = 0; i < nP; ++i)
-        for (int j = 0; j < nP; ++j) T[i][j] = 0;
-    for (int i = 0; i < nP; ++i) {
-        if (i == 0)
-            T[i][i] = 1.0 / es->alphas[i];
-        else
-            T[i][i] = 1.0 / es->alphas[i] + es->betas[i] / es->alphas[i - 1];
-        if (i < nP - 1) T[i][i + 1] = sqrt(es->betas[i + 1]) / es->alphas[i];
-        if (i > 0) T[i][i - 1] = T[i - 1][i];
-    }
-    double xBegin = 0.0, xEnd = 0.0;
-    for (int i = 0; i < nP; ++i) {
-        double Tr = (i == nP - 1) ? 0 : T[i][i + 1];
-        double Tl = (i == 0) ? 0 : T[i][i - 1];
-        double lambMax = T[i][i] + fabs(Tr) + fabs(Tl);
-        double lambMin = T[i][i] - fabs(Tr) - fabs(Tl);
-        xBegin = (xBegin >= lambMin) ? lambMin : xBegin;
-        xEnd = (xEnd <= lambMax) ? lambMax : xEnd;
-    }
-    double p[16];
-    double xn = 0.0;
-    int guard = 0;
-    do {
-        xn = (xBegin + xEnd) * 0.5;
-        int s = 0;
-        p[0] = xn - T[0][0];
-        if (p[0] < 0) s = 1;
-        p[1] = (xn - T[1][1]) * p[0] - T[0][1] * T[0][1];
-        if (p[1] * p[0] < 0) s++;
-        for (int k = 2; k < nP; ++k) {
-            p[k] = (xn - T[k][k]) * p[k - 1] - T[k - 1][k] * T[k - 1][k] * p[k - 2];
-            if (p[k] * p[k - 1] < 0) s++;
-        }
-        if (s >= 1)
-            xBegin = xn;
-        else
-            xEnd = xn;
-    } while ((xEnd - xBegin) >= 0.00001 && ++guard < 4096);
-    es->maxEig = xn;
-}
-
 // ---- chebySmoother::smooth (chebySmoother.cpp:44-148) ---------------------
 __device__ __forceinline__ void cheby_coeffs(double maxEigPCG, int k, double& dtemp1,
                                              double& dtemp2, double& Rtheta)
@@ -304,8 +257,7 @@ void MgSolver::eigen_estimate(int slot, int k, double* xk, const double* bk)
     eig_diag_pcg(ex, R, K.rD.p, xk, bk, K.acf.p, K.w.p, K.p.p, es,
                  pool.site(M_EIGWR, nullptr, FIN_RES_ONLY), pool.site(M_EIGA, nullptr, FIN_RES_ONLY),
                  10);
-    tick();
-    eig_sturm_kernel<<<1, 1, 0, ex.s>>>(es, 10);
+    k_eig_sturm(ex, es, 10);
 }
 
 void MgSolver::chebyshev(int slot, int k, double* xk, const double* bk, int nSweeps)

@@ -16,9 +16,13 @@
 //   * matrices with more than kNoAllocMaxCells cells are rejected with
 //     UNAP_CUDA_EINVAL and a message (there is no fallback that allocates);
 //   * host code cannot use the array's name as a device address, so the
-//     first call on each device looks the address up with
-//     cudaGetSymbolAddress (that device current) and keeps it; make that
-//     first call before any stream capture begins;
+//     first call for a matrix on each device looks the address up with
+//     cudaGetSymbolAddress, with the matrix's device current, and keeps it;
+//   * the call runs on the device the matrix was built on whatever device
+//     is current (it makes that one current for the call and restores the
+//     caller's afterwards); it is synchronous -- it returns when its kernels
+//     have finished -- so it must not be called while a stream capture is
+//     active on the calling thread;
 //   * every call uses the same array: calls whose work overlaps on the GPU
 //     (different streams or host threads at the same time) race on it;
 //     calls on one stream, or one after another, are safe.  Both halves are
@@ -44,12 +48,10 @@ namespace {
 std::mutex g_noalloc_mutex;
 double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
-// device address of the scratch array on the current device, looked up once
-// per device with that device current
-double* noalloc_scratch()
+// device address of the scratch array on device `dev` (current), looked up
+// once per device
+double* noalloc_scratch(int dev)
 {
-    int dev = 0;
-    UNAP_CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices) throw std::invalid_argument("device index out of range");
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (!g_noalloc_ptr[dev]) {
@@ -62,6 +64,21 @@ double* noalloc_scratch()
     }
     return g_noalloc_ptr[dev];
 }
+
+// makes `dev` current for its lifetime, then restores the caller's device
+struct DeviceScope {
+    int old = -1;
+    explicit DeviceScope(int dev)
+    {
+        UNAP_CK(cudaGetDevice(&old));
+        if (old != dev) UNAP_CK(cudaSetDevice(dev));
+    }
+    ~DeviceScope()
+    {
+        int cur = -1;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != old && old >= 0) cudaSetDevice(old);
+    }
+};
 
 }  // namespace
 
@@ -80,7 +97,8 @@ extern "C" int unap_cuda_spmv_noalloc(long int handle, const double* x, double* 
             throw std::invalid_argument("unap_cuda_spmv_noalloc: " + std::to_string(n) +
                                         " cells exceed the static scratch limit of " +
                                         std::to_string(kNoAllocMaxCells));
-        double* scratch = noalloc_scratch();
+        DeviceScope scope(A.device);
+        double* scratch = noalloc_scratch(A.device);
         double* xi = scratch;
         double* yi = scratch + kNoAllocMaxCells;
         Exec ex{A.stream, device_max_blocks()};

@@ -179,6 +179,10 @@ struct Level {
     std::vector<int> waveStart;  // nWave+1, internal row ranges
     std::vector<int> perm;       // internal -> reference cell
     std::vector<int> iperm;      // reference cell -> internal
+    // reference cell -> rank in the locality order (the key order, or the
+    // BFS order of the finest level): internal order within a wavefront,
+    // and the whole internal order of a level built without wavefronts
+    std::vector<int> locRank;
     int nSlices = 0;
     long long nEntries = 0;      // padded SELL storage
     int maxRowLen = 0;
@@ -202,13 +206,16 @@ void update_level_values(Level& L, const HostLdu& A, cudaStream_t s);
 // `key` (optional, size n) gives the locality order inside a wavefront;
 // when empty a BFS order of the matrix graph is used.  `identityOrder`
 // keeps the reference numbering (used for the dense coarsest level).
+// wavefronts == false puts every row in one range in locality order (for
+// levels that are never swept: SpMV-shaped smoothing only); such a level is
+// marked not sweepable.
 std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key,
-                                   bool identityOrder, cudaStream_t s);
+                                   bool identityOrder, cudaStream_t s, bool wavefronts = true);
 void make_fp32(Level& L, cudaStream_t s);
 // The same Level built by kernels on stream s (level_dev.cu); nullptr when
 // the matrix has a shape the device build leaves to the host.
 std::unique_ptr<Level> build_level_device(const HostLdu& A, const std::vector<int>* key,
-                                          cudaStream_t s);
+                                          cudaStream_t s, bool wavefronts = true);
 // Levels of at least this many cells are built on the device (< 0: none).
 long long set_device_setup_min_cells(long long minCells);
 long long device_setup_min_cells();

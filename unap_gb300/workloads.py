@@ -77,6 +77,35 @@ def grid_faces(nx: int, ny: int, nz: int) -> tuple[np.ndarray, np.ndarray]:
     return a, nb[ok]
 
 
+def permuted_grid_faces(nx: int, ny: int, nz: int, perm: np.ndarray):
+    """The faces of an nx*ny*nz hex grid after the cell renumbering
+    c -> perm[c], oriented l < u and sorted by (l, u), with each face's two
+    cells in the natural numbering (a_old -> l, b_old -> u).  Same list as
+    orienting and sorting grid_faces, built row by row (every cell has at
+    most six neighbours) instead of by one sort over all faces."""
+    n = nx * ny * nz
+    perm = perm.astype(np.int32)
+    inv = np.empty(n, dtype=np.int32)
+    inv[perm] = np.arange(n, dtype=np.int32)
+    # row r of the renumbered matrix is old cell inv[r]
+    c = inv.astype(np.int64)
+    i = c % nx
+    j = (c // nx) % ny
+    k = c // (nx * ny)
+    big = np.int32(np.iinfo(np.int32).max)
+    rows = np.arange(n, dtype=np.int32)
+    key = np.full((n, 6), big, dtype=np.int32)
+    for col, (ok, off) in enumerate(((i > 0, -1), (i < nx - 1, 1), (j > 0, -nx), (j < ny - 1, nx),
+                                     (k > 0, -nx * ny), (k < nz - 1, nx * ny))):
+        nb = perm[np.where(ok, c + off, 0)]
+        key[:, col] = np.where(ok & (nb > rows), nb, big)
+    key.sort(axis=1)
+    valid = key != big
+    u = key[valid]
+    l = np.broadcast_to(rows[:, None], key.shape)[valid]
+    return l, u, inv[l].astype(np.int64), inv[u].astype(np.int64)
+
+
 def _orient_and_sort(n: int, a: np.ndarray, b: np.ndarray, perm: np.ndarray | None,
                      *face_data: np.ndarray):
     """Apply the cell permutation, orient l < u and sort faces by (l, u).
@@ -94,6 +123,15 @@ def _orient_and_sort(n: int, a: np.ndarray, b: np.ndarray, perm: np.ndarray | No
     out = [l[order].astype(np.int32), u[order].astype(np.int32), flip[order]]
     out += [d[order] for d in face_data]
     return out
+
+
+def _grid_ldu(nx, ny, nz, perm):
+    """(lowerAddr, upperAddr) of a grid, optionally renumbered by perm."""
+    if perm is None:
+        a, b = grid_faces(nx, ny, nz)
+        return a.astype(np.int32), b.astype(np.int32)
+    l, u, _, _ = permuted_grid_faces(nx, ny, nz, perm)
+    return l, u
 
 
 def _row_abs_sum(n: int, l: np.ndarray, u: np.ndarray, upper: np.ndarray,
@@ -118,8 +156,7 @@ def laplace(nx: int, ny: int | None = None, nz: int | None = None, *, seed: int 
     n = nx * ny * nz
     rng = np.random.default_rng(seed)
     perm = rng.permutation(n).astype(np.int64) if permute else None
-    a, b = grid_faces(nx, ny, nz)
-    l, u, _ = _orient_and_sort(n, a, b, perm)
+    l, u = _grid_ldu(nx, ny, nz, perm)
     upper = np.full(l.shape[0], -1.0)
     diag = _fast_row_abs_sum(n, l, u, upper, upper) + shift
     rhs_v = _rhs(rng, n, rhs)
@@ -135,8 +172,7 @@ def convdiff(nx: int, ny: int | None = None, nz: int | None = None, *, seed: int
     n = nx * ny * nz
     rng = np.random.default_rng(seed)
     perm = rng.permutation(n).astype(np.int64) if permute else None
-    a, b = grid_faces(nx, ny, nz)
-    l, u, _ = _orient_and_sort(n, a, b, perm)
+    l, u = _grid_ldu(nx, ny, nz, perm)
     flux = rng.standard_normal(l.shape[0]) * pe
     upper = -(d + np.maximum(0.0, -flux))
     lower = -(d + np.maximum(0.0, flux))
@@ -154,10 +190,14 @@ def lognormal(nx: int, ny: int | None = None, nz: int | None = None, *, seed: in
     rng = np.random.default_rng(seed)
     perm = rng.permutation(n).astype(np.int64) if permute else None
     kappa = np.exp(rng.standard_normal(n) * sigma)
-    a, b = grid_faces(nx, ny, nz)
+    if perm is not None:
+        l, u, a, b = permuted_grid_faces(nx, ny, nz, perm)
+    else:
+        a, b = grid_faces(nx, ny, nz)
+        l, u = a.astype(np.int32), b.astype(np.int32)
+    # the harmonic mean is symmetric in the two cells
     ka, kb = kappa[a], kappa[b]
     coef = 2.0 * ka * kb / (ka + kb)
-    l, u, _, coef = _orient_and_sort(n, a, b, perm, coef)
     upper = -coef
     diag = _fast_row_abs_sum(n, l, u, upper, upper) + shift
     rhs_v = rng.standard_normal(n)
