@@ -466,6 +466,14 @@ int unap_cuda_set_packed_sweeps(int mode);
  * CTAs would be (default 100000).  Results are identical.  Returns the
  * previous setting.  No counterpart in the reference. */
 int unap_cuda_set_cheby_small_rows(int rows);
+/* Matrices created afterwards (any C ABI call that builds one) get
+ * wavefront ranges for DIC/DILU/Gauss-Seidel sweeps (1, default), or only a
+ * locality order (0): cheaper to build and faster for SpMV gathers, but
+ * only SpMV-shaped work runs on them -- SpMV, Krylov solves without a
+ * preconditioner or with Diag, AMG-PCG with Chebyshev from level 0; the
+ * sweeps return UNAP_CUDA_EINVAL.  Returns the previous setting.  No
+ * counterpart in the reference. */
+int unap_cuda_set_matrix_wavefronts(int on);
 /* Entries of a row the Chebyshev step loads per dependent round trip: 0
  * (default) 16 on levels averaging more than 8 entries per row and 8
  * elsewhere, or 8 / 16 everywhere (fewer registers and more resident warps

@@ -159,3 +159,87 @@ def test_cheby_rejects_bad_parameters(cuda):
         with pytest.raises(capi.UnapCudaError, match=msg):
             capi.DeviceAmg(A, **kw)
     A.close()
+
+
+def test_reference_cheby_smoother_c_abi(cuda, orc):
+    """chebySmoother::smooth through unap_cuda_cheby_smooth_host (the
+    reference's smoother, chebySmoother.cpp:13-149): the first call's
+    eigenvalue estimate (eigenDiagPCG.cpp:11-361) equals the oracle's within
+    the bisection band and leaves x as the oracle's 10 diagonal-PCG
+    iterations do, up to dot-product summation order (1e-12 relative); the
+    next call's Chebyshev sweeps equal the oracle's chain bit for bit from
+    the device's state; on symmetric and asymmetric matrices."""
+    import ctypes
+    lib = capi.load()
+    for s in (W.lognormal(14, 12, 10, seed=5, permute=True),
+              W.convdiff(10, 9, 8, seed=3, permute=True, pe=2.0),
+              W.laplace(12, seed=4, permute=False, rhs="normal")):
+        h = capi.ldumatrixcreat(s)
+        x0 = np.random.default_rng(s.n).standard_normal(s.n)
+        b = np.ascontiguousarray(s.b)
+        x = x0.copy()
+        lam = ctypes.c_double(0.0)
+        est = ctypes.c_int(0)
+        capi.check(lib.unap_cuda_cheby_smooth_host(h, x.ctypes.data, b.ctypes.data, 3,
+                                                   ctypes.byref(lam), ctypes.byref(est)))
+        assert est.value == 1
+        lam_ref, x_ref = orc.eigen(s, x0, b)
+        assert abs(lam.value - lam_ref) <= EIG_TOL, (s.name, lam.value, lam_ref)
+        assert np.linalg.norm(x - x_ref) <= 1e-12 * np.linalg.norm(x_ref), s.name
+        x1 = x.copy()
+        capi.check(lib.unap_cuda_cheby_smooth_host(h, x.ctypes.data, b.ctypes.data, 3,
+                                                   ctypes.byref(lam), ctypes.byref(est)))
+        assert np.array_equal(x, orc.cheby_chain(s, x1, b, lam.value, 1.5, 3)), s.name
+        capi.sw_matrix_destroy(h)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_matrix_without_wavefronts(cuda, orc, precision):
+    """Matrices built in locality order only (unap_cuda_set_matrix_wavefronts
+    (0)): one row range, the same order from the device and the host build,
+    SpMV and the all-Chebyshev V-cycle bit-identical to the oracle, the
+    Krylov solve without a preconditioner within 10% of the oracle's
+    iteration count; the sweeps (DIC, Gauss-Seidel, AMG with Gauss-Seidel
+    on the finest level) refused."""
+    torch = cuda
+    old = capi.set_matrix_wavefronts(False)
+    try:
+        for s in (W.lognormal(14, 12, 10, seed=5, permute=True),
+                  W.lognormal(40, 36, 30, seed=9, permute=True)):
+            A = capi.DeviceMatrix(s)
+            perm, waves = A.layout()
+            assert len(waves) == 2 and waves[-1] == s.n
+            oldd = capi.set_device_setup(-1)
+            try:
+                H = capi.DeviceMatrix(s)
+                assert np.array_equal(H.layout()[0], perm)
+                H.close()
+            finally:
+                capi.set_device_setup(oldd)
+            v = np.random.default_rng(s.n).standard_normal(s.n)
+            y = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+            A.spmv(dev(torch, v), y)
+            assert np.array_equal(y.cpu().numpy(), orc.spmv(s, v))
+            with pytest.raises(capi.UnapCudaError, match="wavefronts"):
+                A.precondition(2, dev(torch, v), y)
+            with pytest.raises(capi.UnapCudaError, match="wavefronts"):
+                A.gauss_seidel(y, dev(torch, v), 1)
+            with pytest.raises(capi.UnapCudaError, match="wavefronts"):
+                capi.DeviceAmg(A, n_coarsest=40, precision=precision)
+            G = capi.DeviceAmg(A, n_coarsest=40, precision=precision, smoother=1, cheby_from=0)
+            O = OracleAmg(orc, s, n_coarsest=40, precision=precision, smoother=1, cheby_from=0,
+                          eig_ratio=30.0)
+            O.set_eigs(G.eigenvalues())
+            z = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+            G.vcycle(dev(torch, v), z)
+            assert np.array_equal(z.cpu().numpy(), O.vcycle(v)), (s.name, precision)
+            G.close()
+            O.close()
+            x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+            st = A.krylov_solve(0, 0, x, dev(torch, s.b), rel_tol=1e-6, max_iter=3000)
+            x_ref, st_ref = orc.pcg(s, 0, s.b, rel_tol=1e-6, max_iter=3000)
+            # unpreconditioned CG amplifies summation-order rounding
+            assert abs(st["nIterations"] - st_ref["n_iter"]) <= max(1, st_ref["n_iter"] // 10)
+            A.close()
+    finally:
+        capi.set_matrix_wavefronts(old)

@@ -113,6 +113,7 @@ SIGNATURES = {
     "unap_cuda_amg_profile_smoother": (_c_int, [_c_long, _c_int, _c_int, _vp, _vp, _vp]),
     "unap_cuda_set_cheby_small_rows": (_c_int, [_c_int]),
     "unap_cuda_set_cheby_chunk": (_c_int, [_c_int]),
+    "unap_cuda_set_matrix_wavefronts": (_c_int, [_c_int]),
     "unap_cuda_amg_profile_vcycle": (_c_int, [_c_long, _c_int, _vp, _c_int, _ip]),
     "unap_cuda_amg_solve": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
     "unap_cuda_amg_solve_host": (_c_int, [_c_long, _vp, _vp, ctypes.POINTER(Stats)]),
@@ -326,6 +327,12 @@ def set_cheby_small_rows(rows: int) -> int:
     """Chebyshev-step launches on levels of at most `rows` rows use one-warp
     CTAs; returns the previous threshold."""
     return int(load().unap_cuda_set_cheby_small_rows(int(rows)))
+
+
+def set_matrix_wavefronts(on: bool) -> bool:
+    """Wavefront ranges for matrices created afterwards (False: locality
+    order only, SpMV-shaped work only); returns the previous value."""
+    return bool(load().unap_cuda_set_matrix_wavefronts(1 if on else 0))
 
 
 def set_cheby_chunk(entries: int) -> int:

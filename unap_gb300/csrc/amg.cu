@@ -34,8 +34,6 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
 {
     auto t0 = std::chrono::steady_clock::now();
     if (!A.host.symm) throw std::invalid_argument("AMG-PCG needs a symmetric matrix");
-    if (!A.L->sweepable)
-        throw std::invalid_argument("AMG smoothing needs oriented, owner-sorted faces");
     if (params.smoother != 0 && params.smoother != 1)
         throw std::invalid_argument("smoother must be 0 (Gauss-Seidel) or 1 (Chebyshev)");
     if (params.smoother == 1) {
@@ -46,6 +44,11 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
         if (!(params.eigRatio > 1.0))
             throw std::invalid_argument("Chebyshev eigenvalue ratio must be > 1");
     }
+    // Gauss-Seidel on the finest level sweeps the matrix's wavefronts
+    if (!A.L->sweepable && !(params.smoother == 1 && params.chebyFrom == 0))
+        throw std::invalid_argument(
+            "AMG Gauss-Seidel smoothing needs oriented, owner-sorted faces and a matrix built "
+            "with wavefronts");
     cudaStream_t s = A.stream;
     std::vector<double> w = mg_face_weights(A.host);
     std::vector<CoarseHost> coarse =

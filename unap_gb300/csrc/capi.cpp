@@ -20,7 +20,7 @@ Matrix& MatHandle::get()
 {
     if (!M) {
         if (!hasValues) throw std::invalid_argument("matrix coefficients were never filled");
-        M = std::make_unique<Matrix>(std::move(pending), nullptr);
+        M = std::make_unique<Matrix>(std::move(pending), nullptr, matrix_wavefronts() != 0);
     }
     return *M;
 }
@@ -583,7 +583,9 @@ int unap_cuda_gauss_seidel(long int handle, double* x, const double* b, int nSwe
         MatHandle* h = mat_from(handle);
         Matrix& A = h->get();
         if (!A.L->sweepable)
-            throw std::invalid_argument("Gauss-Seidel needs oriented, owner-sorted faces");
+            throw std::invalid_argument(
+                "Gauss-Seidel needs oriented, owner-sorted faces and a matrix built with "
+                "wavefronts");
         Exec ex{A.stream, device_max_blocks()};
         h->ensureScratch();
         k_to_internal<double>(ex, A.n(), A.L->d_perm.p, x, h->s1.p);

@@ -28,7 +28,11 @@ void set_last_error(const std::string& msg) { g_last_error = msg; }
 const char* last_error() { return g_last_error.c_str(); }
 
 // ---- Matrix ----------------------------------------------------------------
-Matrix::Matrix(HostLdu&& h, cudaStream_t s) : host(std::move(h)), stream(s)
+static std::atomic<int> g_matrixWavefronts{1};
+int set_matrix_wavefronts(int on) { return g_matrixWavefronts.exchange(on ? 1 : 0); }
+int matrix_wavefronts() { return g_matrixWavefronts.load(); }
+
+Matrix::Matrix(HostLdu&& h, cudaStream_t s, bool wavefronts) : host(std::move(h)), stream(s)
 {
     UNAP_CK(cudaGetDevice(&device));
     if (!stream) {
@@ -36,7 +40,7 @@ Matrix::Matrix(HostLdu&& h, cudaStream_t s) : host(std::move(h)), stream(s)
         ownsStream = true;
     }
     host.validate();
-    L = build_level(host, nullptr, false, stream);
+    L = build_level(host, nullptr, false, stream, wavefronts);
 }
 
 Matrix::~Matrix()
@@ -131,7 +135,8 @@ public:
     {
         if (!L.sweepable)
             throw std::invalid_argument(
-                "DIC/DILU need faces oriented lowerAddr < upperAddr and sorted by owner");
+                "DIC/DILU need faces oriented lowerAddr < upperAddr and sorted by owner, "
+                "and a matrix built with wavefronts");
         Exec ex;
         ex.s = A.stream;
         ex.maxBlocks = device_max_blocks();

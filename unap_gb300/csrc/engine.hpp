@@ -21,7 +21,10 @@ struct SolveStats {
 // reference layout; the device Level holds the internal order and SELL rows.
 class Matrix {
 public:
-    Matrix(HostLdu&& h, cudaStream_t s);
+    // wavefronts == false: locality order without wavefront ranges, for a
+    // matrix used only by SpMV-shaped work (SpMV, Chebyshev smoothing,
+    // AMG without Gauss-Seidel on it); DIC, DILU and Gauss-Seidel refuse it
+    Matrix(HostLdu&& h, cudaStream_t s, bool wavefronts = true);
     ~Matrix();
     HostLdu host;
     std::unique_ptr<Level> L;
@@ -107,6 +110,10 @@ private:
 
 // default executor of Krylov objects created afterwards; returns the old one
 int set_default_executor(int persistent);
+// whether matrices created through the C ABI afterwards get wavefront
+// ranges (1, default) or only a locality order (0); returns the old value
+int set_matrix_wavefronts(int on);
+int matrix_wavefronts();
 
 // Dense FP64 SPD inverse by Cholesky (row-major in, row-major out).
 // Returns false when the matrix is not positive definite.

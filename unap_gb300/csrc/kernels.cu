@@ -258,35 +258,57 @@ void dic_factor(const Exec& ex, const Level& L, bool dilu, double* dfac, double*
 
 // forward sweep (lduDICPrecond.cpp:63-71; DILU in losort order,
 // lduDILUPrecond.cpp:70-80): w_c = rD_c r_c - sum_low (rD_c coef) w_l
+template <int CK>
 __global__ void __launch_bounds__(kBlock) dic_fwd_kernel(Rows<double> A, const double* coef,
                                                          const double* __restrict__ rD,
-                                                         const double* __restrict__ rr,
-                                                         double* w, int r0, int r1, Gate g)
+                                                         const double* rr, double* w, int r0,
+                                                         int r1, Gate g)
 {
-    if (gate_closed(g)) return;
-    for (int r = r0 + blockIdx.x * blockDim.x + threadIdx.x; r < r1;
-         r += gridDim.x * blockDim.x) {
-        const int info = ldg(A.rowInfo + r);
-        const int nLow = info >> 16;
-        const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
-        const double rd = ldg(rD + r);
-        double acc = rd * ldg(rr + r);
-        for (int j = 0; j < nLow; ++j) {
-            const int e = base + 32 * j;
-            acc -= rd * ldg(coef + e) * w[ldg(A.col + e)];
+    // Programmatic dependent launch: the next wavefront's kernel may launch
+    // now.  Before griddepcontrol.wait this kernel reads only the matrix and
+    // rD (written at factorisation); r, w and the solver state after it.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const int r = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+    int nLow = 0, base = 0;
+    double rd = 0.0;
+    int c[CK];
+    double v[CK];
+    if (r < r1) {
+        nLow = ldg(A.rowInfo + r) >> 16;
+        base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
+        rd = ldg(rD + r);
+#pragma unroll
+        for (int k = 0; k < CK; ++k) {
+            const int e = base + 32 * k;
+            c[k] = k < nLow ? ldg(A.col + e) : r;
+            v[k] = k < nLow ? ldg(coef + e) : 0.0;
         }
-        w[r] = acc;
     }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (gate_closed(g) || r >= r1) return;
+    // lduDICPrecond.cpp:65-71: w = rD r, then w_u -= (rD_u coef) w_l in face order
+    double acc = rd * rr[r];
+#pragma unroll
+    for (int k = 0; k < CK; ++k)
+        if (k < nLow) acc -= rd * v[k] * w[c[k]];
+    for (int j = CK; j < nLow; ++j) {
+        const int e = base + 32 * j;
+        acc -= rd * ldg(coef + e) * w[ldg(A.col + e)];
+    }
+    w[r] = acc;
 }
 
 // backward sweep (lduDICPrecond.cpp:73-76): faces in reverse order,
 // w_c -= (rD_c upper) w_u; sums w.r for the PCG/PBiCGStab dot product
 __global__ void __launch_bounds__(kBlock) dic_bwd_kernel(Rows<double> A,
                                                          const double* __restrict__ rD,
-                                                         const double* __restrict__ rr,
-                                                         double* w, int r0, int r1, RSpec red,
-                                                         Gate g)
+                                                         const double* rr, double* w, int r0,
+                                                         int r1, RSpec red, Gate g)
 {
+    // programmatic dependent launch: launch the next wavefront now, wait for
+    // this one's inputs before reading anything the chain writes
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     if (gate_closed(g)) return;
     double v[1] = {0.0};
     for (int r = r0 + blockIdx.x * blockDim.x + threadIdx.x; r < r1;
@@ -302,10 +324,14 @@ __global__ void __launch_bounds__(kBlock) dic_bwd_kernel(Rows<double> A,
             acc -= rd * ldg(A.val + e) * w[ldg(A.col + e)];
         }
         w[r] = acc;
-        v[0] += acc * ldg(rr + r);
+        v[0] += acc * rr[r];
     }
     if (red.blockPart) reduce_and_finalize<1>(v, red);
 }
+
+// wavefronts of up to this many rows launch one-warp CTAs (spread over more
+// SMs, as for the Gauss-Seidel wavefronts)
+constexpr int kDicSmallRows = 100000;
 
 void dic_apply(const Exec& ex, const Level& L, bool dilu, const double* rD, const double* r,
                double* w, const RedPool* pool, int site, KState* st, int fin, Gate g)
@@ -313,21 +339,38 @@ void dic_apply(const Exec& ex, const Level& L, bool dilu, const double* rD, cons
     Rows<double> A = rows64(L);
     const double* coef = dilu ? A.val : A.valT;  // DIC uses upper on the lower side
     const int W = L.nWave;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.stream = ex.s;
+    cfg.attrs = at;
+    cfg.numAttrs = wave_pdl() ? 1 : 0;
     for (int k = 0; k < W; ++k) {
-        int r0 = L.waveStart[k], r1 = L.waveStart[k + 1];
-        if (r1 > r0)
-            tick(), dic_fwd_kernel<<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, coef, rD, r, w, r0, r1, g);
+        const int r0 = L.waveStart[k], r1 = L.waveStart[k + 1];
+        if (r1 <= r0) continue;
+        const int threads = (r1 - r0) <= kDicSmallRows ? 32 : kBlock;
+        cfg.gridDim = dim3((unsigned)div_up(r1 - r0, threads));
+        cfg.blockDim = dim3((unsigned)threads);
+        tick();
+        UNAP_CK(cudaLaunchKernelEx(&cfg, dic_fwd_kernel<4>, A, coef, rD, r, w, r0, r1, g));
     }
     // backward: one launch slot per non-empty wavefront
     int nonEmpty = 0;
     for (int k = 0; k < W; ++k) nonEmpty += L.waveStart[k + 1] > L.waveStart[k];
     int slot = 0;
     for (int k = W - 1; k >= 0; --k) {
-        int r0 = L.waveStart[k], r1 = L.waveStart[k + 1];
+        const int r0 = L.waveStart[k], r1 = L.waveStart[k + 1];
         if (r1 <= r0) continue;
         RSpec red;
         if (pool) red = pool->site(site, st, slot == nonEmpty - 1 ? fin : FIN_STORE, slot, nonEmpty);
-        tick(), dic_bwd_kernel<<<ex.grid(r1 - r0), kBlock, 0, ex.s>>>(A, rD, r, w, r0, r1, red, g);
+        const int threads = (r1 - r0) <= kDicSmallRows ? 32 : kBlock;
+        int grid = div_up(r1 - r0, threads);
+        if (red.blockPart && grid > red.maxBlocks) grid = red.maxBlocks;
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3((unsigned)threads);
+        tick();
+        UNAP_CK(cudaLaunchKernelEx(&cfg, dic_bwd_kernel, A, rD, r, w, r0, r1, red, g));
         ++slot;
     }
 }

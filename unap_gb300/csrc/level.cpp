@@ -163,6 +163,19 @@ std::unique_ptr<Level> build_level(const HostLdu& A, const std::vector<int>* key
         std::vector<int> pos(L->waveStart.begin(), L->waveStart.end() - 1);
         for (int c : byKey) L->perm[(size_t)pos[(size_t)wave[(size_t)c]]++] = c;
         L->nWave = nWave;
+        if (!wavefronts) {
+            // rows of similar length share SELL-32 slices: inside every
+            // window of 256 rows, decreasing row length (stable)
+            auto deg = [&](int c) {
+                return loStart[(size_t)c + 1] - loStart[(size_t)c] + ownStart[(size_t)c + 1] -
+                       ownStart[(size_t)c];
+            };
+            for (int w0 = 0; w0 < n; w0 += 256) {
+                const int w1 = std::min(n, w0 + 256);
+                std::stable_sort(L->perm.begin() + w0, L->perm.begin() + w1,
+                                 [&](int a, int b) { return deg(a) > deg(b); });
+            }
+        }
     }
     for (int i = 0; i < n; ++i) L->iperm[(size_t)L->perm[(size_t)i]] = i;
 

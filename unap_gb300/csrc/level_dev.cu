@@ -405,6 +405,28 @@ __global__ void k_split_scan(int* cnt, long long nChunks, int nWave, int* total)
     total[w] = run;
 }
 
+// Rows of a level without wavefronts, reordered inside every window of
+// kLenWindow internal rows by decreasing row length (stable), so that
+// SELL-32 slices hold rows of similar length: one CTA per window.
+constexpr int kLenWindow = 256;
+
+__global__ void __launch_bounds__(kLenWindow) k_window_by_length(Adj adj, int n, int* perm)
+{
+    __shared__ int cell[kLenWindow], len[kLenWindow];
+    const int w0 = blockIdx.x * kLenWindow;
+    const int m = min(kLenWindow, n - w0);
+    const int t = threadIdx.x;
+    if (t < m) {
+        cell[t] = perm[w0 + t];
+        len[t] = adj.deg(cell[t]);
+    }
+    __syncthreads();
+    int rank = 0;
+    if (t < m)
+        for (int j = 0; j < m; ++j) rank += (len[j] > len[t]) || (len[j] == len[t] && j < t);
+    if (t < m) perm[w0 + rank] = cell[t];
+}
+
 __global__ void k_iperm(const int* __restrict__ perm, int n, int* iperm)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -702,6 +724,9 @@ std::unique_ptr<Level> build_level_device(const HostLdu& A, const std::vector<in
         exclusive_scan(tot.p, ws.p, nWave, s);
         k_split<true><<<warpsGrid, kThreads, 0, s>>>(byKey.p, wave.p, n, nWave, cnt.p, ws.p, L->d_perm.p);
     }
+    if (!wavefronts)
+        k_window_by_length<<<(n + kLenWindow - 1) / kLenWindow, kLenWindow, 0, s>>>(adj, n,
+                                                                                L->d_perm.p);
     k_iperm<<<grid_for(n), kThreads, 0, s>>>(L->d_perm.p, n, L->d_iperm.p);
     Scratch<int> locRank((size_t)n, s);
     k_iperm<<<grid_for(n), kThreads, 0, s>>>(byKey.p, n, locRank.p);

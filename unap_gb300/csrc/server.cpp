@@ -134,7 +134,10 @@ void Server::largeWorker()
         }
         r->tStart = now_seconds();
         try {
-            Matrix A(std::move(r->A), s);
+            // AMG requests smooth every level by Chebyshev steps: their
+            // matrix needs no wavefronts (cheaper setup, local gathers)
+            const bool amgReq = r->method == SERVE_AMG_MIXED || r->method == SERVE_AMG_FP64;
+            Matrix A(std::move(r->A), s, !amgReq);
             const size_t n = (size_t)A.n();
             DevArray<double> dx(n), db(n);
             db.upload(r->b, s);
