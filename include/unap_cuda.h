@@ -368,11 +368,13 @@ int unap_cuda_mg_set(long int mg, int nPre, int nPost, int nFinest, int scaleCor
 int unap_cuda_mg_destroy(long int mg);
 
 /* ---- Batched solves of many systems of uneven size.  Systems of at most
- * 65,536 cells are solved together in one launch (one CTA runs one system's
- * whole PCG / PBiCGStab solve); larger ones one after another with the
- * per-system driver.  The CTA size of the fused launch is chosen by the
- * autotuner (first batch of each size class times 128/256/512/1024
- * threads).  x and b are device pointers in each system's cell order. */
+ * 65,536 cells (unap_cuda_set_team_solve_cells) are solved together in one
+ * launch: a team of CTAs per system (one CTA, or a thread-block cluster of
+ * 2 to 16) runs that system's whole PCG / PBiCGStab solve; larger ones run
+ * one after another with the per-system driver.  The launch shape (CTA size
+ * x CTAs per system) is chosen by the autotuner: the first batch of each
+ * (size class, count class) times every launchable shape.  x and b are
+ * device pointers in each system's cell order. */
 typedef struct {
     long int matrix; /* handle from unap_cuda_matrix_create / ldumatrixcreat_ */
     int method;      /* 0 PCG, 1 PBiCGStab */
@@ -387,6 +389,22 @@ int unap_cuda_batch_create(long int* batch);
 int unap_cuda_batch_solve(long int batch, int count, const unap_cuda_batch_item* items,
                           unap_cuda_stats* stats, int* ctaThreads);
 int unap_cuda_batch_destroy(long int batch);
+/* launch shape of the batch's last fused launch: CTA size, CTAs per system */
+int unap_cuda_batch_last_shape(long int batch, int* ctaThreads, int* clusterCtas);
+/* Systems of at most `cells` cells with an LDU preconditioner (none, Diag,
+ * DIC, DILU) are solved by one whole-solve launch, in batches and by
+ * unap_cuda_krylov_solve / pcgsolversolve_ / pbicgstabsolversolve_ alike
+ * (default 65,536; 0 turns it off).  Returns the previous value; it applies
+ * to solvers created afterwards. */
+int unap_cuda_set_team_solve_cells(int cells);
+/* the autotuner's cached shape for `systems` systems of up to `cells`
+ * cells ({0, 0}: not tuned yet) */
+int unap_cuda_team_shape(int cells, int systems, int* ctaThreads, int* clusterCtas);
+/* every later whole-solve launch uses this shape (CTA size 128, 256, 512 or
+ * 1024; cluster 1, 2, 4, 8 or 16 CTAs) instead of the autotuner's; a shape
+ * the device cannot schedule is an error.  ctaThreads = 0 returns to the
+ * autotuner. */
+int unap_cuda_force_team_shape(int ctaThreads, int clusterCtas);
 
 /* ---- Continuous-batching solve server.  Requests carry their own matrix
  * (host arrays, copied) and right-hand side; method 0 mixed AMG-PCG, 1 FP64
@@ -415,6 +433,10 @@ int unap_cuda_server_submit(long int server, int nCells, int nFaces, const int* 
                             int maxIter, long long* id);
 int unap_cuda_server_wait(long int server, long long id, double* x, unap_cuda_request_info* info);
 int unap_cuda_server_destroy(long int server);
+/* server slots replay each Krylov iteration from a CUDA graph (1, the
+ * default) or launch its kernels one by one (0); applies to requests started
+ * afterwards; returns the previous setting */
+int unap_cuda_set_server_graphs(int on);
 
 int unap_cuda_device_synchronize(void);
 

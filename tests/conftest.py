@@ -27,14 +27,17 @@ def ref():
     return Oracle("ref")
 
 
-@pytest.fixture(params=["persistent", "graph"])
+@pytest.fixture(params=["persistent", "graph", "team"])
 def executor(request, cuda):
-    """Runs a test once with the persistent step executor and once with
-    per-step kernel launches captured in a CUDA graph."""
+    """Runs a test with the persistent step executor, with per-step kernel
+    launches captured in a CUDA graph (whole-solve launches off for both),
+    and with small Krylov solves in one whole-solve launch."""
     from unap_gb300 import capi
     old = capi.set_executor(request.param == "persistent")
+    cells = capi.set_team_solve_cells(1 << 20 if request.param == "team" else 0)
     yield request.param
     capi.set_executor(old)
+    capi.set_team_solve_cells(cells)
 
 
 TAIL_MODES = {

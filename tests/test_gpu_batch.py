@@ -88,3 +88,75 @@ def test_batch_factor_cache_after_matrix_replaced(cuda, orc):
         assert abs(st["nIterations"] - st_ref["n_iter"]) <= 1, (seed, st, st_ref)
         m.close()
     B.close()
+
+
+def team_cases():
+    return [(W.laplace(20, 18, 16, seed=51, permute=True, rhs="normal", shift=0.1), 0, 2),
+            (W.laplace(24, 24, 24, seed=52, permute=False, rhs="uniform"), 0, 2),
+            (W.lognormal(16, 15, 14, seed=53, permute=True, sigma=1.0, shift=0.01), 0, 1),
+            (W.convdiff(18, 17, 16, seed=54, permute=True, pe=4.0), 1, 3),
+            (W.convdiff(12, 12, 30, seed=55, permute=False, pe=2.0), 1, 3),
+            (W.laplace(15, 14, 13, seed=56, permute=True, shift=0.5), 0, 0)]
+
+
+@pytest.mark.parametrize("threads,cluster", [(128, 1), (1024, 1), (256, 2), (512, 4),
+                                             (128, 8), (1024, 8), (256, 16), (1024, 16)])
+def test_team_shapes_match_oracle(cuda, orc, threads, cluster):
+    """Every launch shape of the whole-solve kernel (one CTA, or a cluster of
+    2-16 CTAs whose block sums meet in distributed shared memory) gives the
+    oracle's iterations within one and its solution in residual space, and
+    a repeated launch of the same shape is bit-identical."""
+    torch = cuda
+    if cluster > 1 and capi.load().unap_cuda_force_team_shape(threads, cluster) != 0:
+        pytest.skip("device cannot schedule this cluster")
+    capi.force_team_shape(threads, cluster)
+    try:
+        cases = team_cases()
+        mats = [capi.DeviceMatrix(s) for s, _, _ in cases]
+        bs = [torch.tensor(s.b, device="cuda") for s, _, _ in cases]
+        B = capi.Batch()
+        runs = []
+        for rep in range(2):
+            xs = [torch.zeros(s.n, dtype=torch.float64, device="cuda") for s, _, _ in cases]
+            items = [dict(matrix=m, method=meth, precond=pc, x=x, b=b, rel_tol=1e-9,
+                          max_iter=2000)
+                     for m, (s, meth, pc), x, b in zip(mats, cases, xs, bs)]
+            stats, _ = B.solve(items)
+            assert B.last_shape() == (threads, cluster)
+            runs.append(([x.cpu().numpy() for x in xs], stats))
+        for (s, meth, pc), st, xb, xb2 in zip(cases, runs[0][1], runs[0][0], runs[1][0]):
+            fn = orc.pcg if meth == 0 else orc.pbicgstab
+            x_ref, st_ref = fn(s, pc, s.b, rel_tol=1e-9, max_iter=2000)
+            assert st["converged"], (s.name, st)
+            assert abs(st["nIterations"] - st_ref["n_iter"]) <= 1, (s.name, st, st_ref)
+            d = orc.spmv(s, xb - x_ref)
+            assert np.linalg.norm(d) <= 2.2e-9 * st_ref["init_res"], s.name
+            assert np.array_equal(xb, xb2), s.name
+        # single solves through the Krylov driver take the same launch
+        s, meth, pc = cases[1]
+        x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+        st = mats[1].krylov_solve(meth, pc, x, bs[1], rel_tol=1e-9, max_iter=2000)
+        assert np.array_equal(x.cpu().numpy(), runs[0][0][1])
+        assert st["nIterations"] == runs[0][1][1]["nIterations"]
+        B.close()
+        for m in mats:
+            m.close()
+    finally:
+        capi.force_team_shape(0, 0)
+
+
+def test_team_shape_autotuner(cuda):
+    """The autotuner picks a launchable shape per (size class, count class)
+    and reuses it."""
+    torch = cuda
+    s = W.laplace(22, 21, 20, seed=61, permute=True, rhs="normal", shift=0.1)
+    m = capi.DeviceMatrix(s)
+    b = torch.tensor(s.b, device="cuda")
+    x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    m.krylov_solve(0, 2, x, b, rel_tol=1e-9, max_iter=2000)
+    t, c = capi.team_shape(s.n, 1)
+    assert t in (128, 256, 512, 1024) and c in (1, 2, 4, 8, 16)
+    x.zero_()
+    m.krylov_solve(0, 2, x, b, rel_tol=1e-9, max_iter=2000)
+    assert capi.team_shape(s.n, 1) == (t, c)
+    m.close()

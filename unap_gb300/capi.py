@@ -146,6 +146,11 @@ SIGNATURES = {
     "unap_cuda_batch_create": (_c_int, [_lp]),
     "unap_cuda_batch_solve": (_c_int, [_c_long, _c_int, _vp, _vp, _ip]),
     "unap_cuda_batch_destroy": (_c_int, [_c_long]),
+    "unap_cuda_batch_last_shape": (_c_int, [_c_long, _ip, _ip]),
+    "unap_cuda_set_team_solve_cells": (_c_int, [_c_int]),
+    "unap_cuda_team_shape": (_c_int, [_c_int, _c_int, _ip, _ip]),
+    "unap_cuda_force_team_shape": (_c_int, [_c_int, _c_int]),
+    "unap_cuda_set_server_graphs": (_c_int, [_c_int]),
     "unap_cuda_server_create": (_c_int, [_lp, _c_ll, _c_int, _c_int]),
     "unap_cuda_server_submit": (_c_int, [_c_long, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp,
                                          _c_int, _c_dbl, _c_int, ctypes.POINTER(_c_ll)]),
@@ -194,6 +199,12 @@ class Batch:
         check(load().unap_cuda_batch_solve(self.handle, len(items), arr, stats,
                                            ctypes.byref(threads)))
         return [s.as_dict() for s in stats], threads.value
+
+    def last_shape(self):
+        """(CTA size, CTAs per system) of the last fused launch."""
+        t, c = ctypes.c_int(0), ctypes.c_int(0)
+        check(load().unap_cuda_batch_last_shape(self.handle, ctypes.byref(t), ctypes.byref(c)))
+        return t.value, c.value
 
     def close(self):
         if self.handle:
@@ -304,6 +315,32 @@ class DeviceMG:
 def set_executor(persistent: bool) -> bool:
     """Executor of PCG solves created afterwards; returns the previous one."""
     return bool(load().unap_cuda_set_executor(1 if persistent else 0))
+
+
+def set_team_solve_cells(cells: int) -> int:
+    """Systems of at most `cells` cells with an LDU preconditioner are solved
+    by one whole-solve launch (0: never); returns the previous value."""
+    return int(load().unap_cuda_set_team_solve_cells(int(cells)))
+
+
+def set_server_graphs(on: bool) -> bool:
+    """Server slots replay Krylov iterations from CUDA graphs (default) or
+    launch kernel by kernel; returns the previous setting."""
+    return bool(load().unap_cuda_set_server_graphs(1 if on else 0))
+
+
+def force_team_shape(threads: int, cluster: int = 1) -> None:
+    """Whole-solve launches use this shape from now on (threads 0: back to
+    the autotuner)."""
+    check(load().unap_cuda_force_team_shape(int(threads), int(cluster)))
+
+
+def team_shape(cells: int, systems: int = 1):
+    """The autotuner's cached (CTA size, CTAs per system) for `systems`
+    systems of up to `cells` cells; (0, 0) when not tuned yet."""
+    t, c = ctypes.c_int(0), ctypes.c_int(0)
+    check(load().unap_cuda_team_shape(int(cells), int(systems), ctypes.byref(t), ctypes.byref(c)))
+    return t.value, c.value
 
 
 def set_wave_pdl(on: bool) -> bool:

@@ -1,19 +1,19 @@
 // Batched solves of many LDU systems of uneven size.
 //
-// Systems of at most kBatchSmallCells cells are solved together in ONE
-// launch: one CTA per system runs the whole PCG or PBiCGStab solve
-// (small_solve.cu), so a batch of hundreds of small systems costs one launch
-// instead of hundreds of iterations x kernels.  Larger systems of the batch
-// are solved one after another with the per-system Krylov driver (persistent
-// step executor for PCG).  Vectors enter and leave in the caller's cell
-// order through one batched gather/scatter launch each.
+// Systems of at most team_solve_cells() cells are solved together in ONE
+// launch: a team of CTAs per system (one CTA, or a thread-block cluster) runs
+// the whole PCG or PBiCGStab solve (small_solve.cu), so a batch of hundreds
+// of small systems costs one launch instead of hundreds of iterations x
+// kernels.  Larger systems of the batch are solved one after another with
+// the per-system Krylov driver.  Vectors enter and leave in the caller's
+// cell order through one batched gather/scatter launch each.
 //
-// The CTA size of the fused launch is picked by an autotuner: the first
-// batch of each size class (largest system rounded up to a power of two) is
-// timed with 128, 256, 512 and 1024 threads per CTA (CUDA events on the
-// batch's stream, x reset between trials) and the fastest is cached for the
-// class.
+// The launch shape (CTA size x CTAs per system) is picked by an autotuner:
+// the first batch of each (size class, count class) is timed with every
+// launchable shape, iterations capped, x reset between trials, and the
+// fastest is cached for the pair.
 #include <algorithm>
+#include <atomic>
 #include <map>
 #include <mutex>
 
@@ -45,7 +45,10 @@ __global__ void batch_perm_kernel(const PermJob* jobs)
 }
 
 std::mutex g_tune_mutex;
-std::map<int, int> g_tuned;  // size class -> threads
+std::map<std::pair<int, int>, TeamShape> g_tuned;  // (size class, count class) -> shape
+std::atomic<int> g_teamCells{kTeamSolveCells};
+std::atomic<int> g_forceThreads{0}, g_forceCluster{0};  // shape override (0: tuner)
+constexpr int kTuneIters = 10;  // iterations per timed trial
 
 int size_class(int n)
 {
@@ -54,13 +57,105 @@ int size_class(int n)
     return c;
 }
 
+int count_class(int m)
+{
+    return m <= 1 ? 1 : m <= 4 ? 4 : m <= 16 ? 16 : m <= 64 ? 64 : 1 << 30;
+}
+
 }  // namespace
 
-int batch_tuned_threads(int sizeClass)
+int team_solve_cells() { return g_teamCells.load(); }
+
+int set_team_solve_cells(int cells) { return g_teamCells.exchange(std::max(cells, 0)); }
+
+void force_team_shape(int threads, int cluster)
 {
+    if (threads && !small_team_size_ok(threads, cluster))
+        throw std::invalid_argument("team shape: threads 128, 256, 512 or 1024; cluster 1, 2, "
+                                    "4, 8 or 16");
+    if (threads && cluster > 1 && small_team_capacity(threads, cluster) <= 0)
+        throw std::invalid_argument("team shape: this cluster cannot be scheduled on the device");
+    g_forceThreads = threads;
+    g_forceCluster = threads ? cluster : 0;
+}
+
+TeamShape cached_team_shape(int nMax, int m)
+{
+    if (g_forceThreads.load()) return TeamShape{g_forceThreads.load(), g_forceCluster.load()};
     std::lock_guard<std::mutex> lock(g_tune_mutex);
-    auto it = g_tuned.find(sizeClass);
-    return it == g_tuned.end() ? 0 : it->second;
+    auto it = g_tuned.find({size_class(nMax), count_class(m)});
+    return it == g_tuned.end() ? TeamShape{0, 0} : it->second;
+}
+
+TeamShape tuned_team_shape(cudaStream_t stream, const SmallSystem* dSys, int m, int nMax)
+{
+    const TeamShape have = cached_team_shape(nMax, m);
+    if (have.threads) return have;
+    std::vector<SmallSystem> sys((size_t)m);
+    UNAP_CK(cudaMemcpyAsync(sys.data(), dSys, sizeof(SmallSystem) * (size_t)m,
+                            cudaMemcpyDeviceToHost, stream));
+    UNAP_CK(cudaStreamSynchronize(stream));
+    // trial copies: iterations capped, no result written; a one-iteration
+    // copy runs first for every shape (loads its kernel) untimed
+    std::vector<SmallSystem> trial = sys, warm = sys;
+    for (auto& S : trial) {
+        S.maxIter = std::min(S.maxIter, kTuneIters);
+        S.minIter = std::min(S.minIter, kTuneIters);
+        S.result = nullptr;
+    }
+    for (auto& S : warm) {
+        S.maxIter = 1;
+        S.minIter = 0;
+        S.result = nullptr;
+    }
+    DevArray<SmallSystem> dTrial, dWarm;
+    dTrial.upload(trial.data(), trial.size(), stream);
+    dWarm.upload(warm.data(), warm.size(), stream);
+    size_t total = 0;
+    for (auto& S : sys) total += (size_t)S.A.n;
+    DevArray<double> x0(total);
+    auto copy_x = [&](bool save) {
+        size_t off = 0;
+        for (auto& S : sys) {
+            double* a = x0.p + off;
+            UNAP_CK(cudaMemcpyAsync(save ? a : S.x, save ? S.x : a, sizeof(double) * (size_t)S.A.n,
+                                    cudaMemcpyDeviceToDevice, stream));
+            off += (size_t)S.A.n;
+        }
+    };
+    copy_x(true);
+    cudaEvent_t e0, e1;
+    UNAP_CK(cudaEventCreate(&e0));
+    UNAP_CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    TeamShape bestS;
+    for (int C : {1, 2, 4, 8, 16}) {
+        for (int t : {128, 256, 512, 1024}) {
+            if (C > 1 && small_team_capacity(t, C) <= 0) continue;
+            copy_x(false);
+            launch_small_krylov(stream, dWarm.p, m, nullptr, t, C);
+            copy_x(false);
+            UNAP_CK(cudaEventRecord(e0, stream));
+            launch_small_krylov(stream, dTrial.p, m, nullptr, t, C);
+            UNAP_CK(cudaEventRecord(e1, stream));
+            UNAP_CK(cudaEventSynchronize(e1));
+            float ms = 0;
+            UNAP_CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                bestS = TeamShape{t, C};
+            }
+        }
+    }
+    copy_x(false);
+    UNAP_CK(cudaStreamSynchronize(stream));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tuned[{size_class(nMax), count_class(m)}] = bestS;
+    }
+    return bestS;
 }
 
 BatchSolver::BatchSolver(cudaStream_t s) : stream(s) {}
@@ -107,7 +202,7 @@ std::vector<SolveStats> BatchSolver::solve(const std::vector<BatchItem>& items)
         const BatchItem& it = items[i];
         if (!it.A->L->sweepable && (it.precond == 2 || it.precond == 3))
             throw std::invalid_argument("DIC/DILU need oriented, owner-sorted faces");
-        (it.A->n() <= kBatchSmallCells ? small : large).push_back((int)i);
+        (it.A->n() <= team_solve_cells() ? small : large).push_back((int)i);
     }
     if (!small.empty()) solveSmall(items, small, out);
     for (int i : large) {
@@ -179,10 +274,8 @@ void BatchSolver::solveSmall(const std::vector<BatchItem>& items, const std::vec
     if (!capturing()) count_launches(1);
     batch_perm_kernel<<<2 * m, 256, 0, stream>>>(reinterpret_cast<const PermJob*>(dIn.p));
 
-    const int cls = size_class(nMax);
-    int threads = batch_tuned_threads(cls);
-    if (!threads) threads = autotune(cls, m);
-    launch_small_krylov(stream, dSys.p, m, nullptr, threads);
+    const TeamShape shape = tuned_team_shape(stream, dSys.p, m, nMax);
+    launch_small_krylov(stream, dSys.p, m, nullptr, shape.threads, shape.cluster);
     if (!capturing()) count_launches(1);
     batch_perm_kernel<<<m, 256, 0, stream>>>(reinterpret_cast<const PermJob*>(dOut.p));
     std::vector<SmallResult> res((size_t)m);
@@ -198,64 +291,7 @@ void BatchSolver::solveSmall(const std::vector<BatchItem>& items, const std::vec
         s.initRes = res[(size_t)j].initRes;
         s.finalRes = res[(size_t)j].finalRes;
     }
-    lastThreads = threads;
-}
-
-int BatchSolver::autotune(int sizeClass, int m)
-{
-    // time each candidate on this batch; x is restored from the gathered
-    // initial guess before every trial (the batch's own solve follows)
-    const int cands[4] = {128, 256, 512, 1024};
-    std::vector<SmallSystem> sys((size_t)m);
-    UNAP_CK(cudaMemcpyAsync(sys.data(), dSys.p, sizeof(SmallSystem) * (size_t)m,
-                            cudaMemcpyDeviceToHost, stream));
-    UNAP_CK(cudaStreamSynchronize(stream));
-    size_t total = 0;
-    for (auto& S : sys) total += (size_t)S.A.n;
-    DevArray<double> x0(total);
-    size_t off = 0;
-    for (auto& S : sys) {
-        UNAP_CK(cudaMemcpyAsync(x0.p + off, S.x, sizeof(double) * (size_t)S.A.n,
-                                cudaMemcpyDeviceToDevice, stream));
-        off += (size_t)S.A.n;
-    }
-    cudaEvent_t e0, e1;
-    UNAP_CK(cudaEventCreate(&e0));
-    UNAP_CK(cudaEventCreate(&e1));
-    float best = 1e30f;
-    int bestT = kSmallBlock;
-    for (int t : cands) {
-        off = 0;
-        for (auto& S : sys) {
-            UNAP_CK(cudaMemcpyAsync(S.x, x0.p + off, sizeof(double) * (size_t)S.A.n,
-                                    cudaMemcpyDeviceToDevice, stream));
-            off += (size_t)S.A.n;
-        }
-        UNAP_CK(cudaEventRecord(e0, stream));
-        launch_small_krylov(stream, dSys.p, m, nullptr, t);
-        UNAP_CK(cudaEventRecord(e1, stream));
-        UNAP_CK(cudaEventSynchronize(e1));
-        float ms = 0;
-        UNAP_CK(cudaEventElapsedTime(&ms, e0, e1));
-        if (ms < best) {
-            best = ms;
-            bestT = t;
-        }
-    }
-    off = 0;
-    for (auto& S : sys) {
-        UNAP_CK(cudaMemcpyAsync(S.x, x0.p + off, sizeof(double) * (size_t)S.A.n,
-                                cudaMemcpyDeviceToDevice, stream));
-        off += (size_t)S.A.n;
-    }
-    UNAP_CK(cudaStreamSynchronize(stream));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    {
-        std::lock_guard<std::mutex> lock(g_tune_mutex);
-        g_tuned[sizeClass] = bestT;
-    }
-    return bestT;
+    lastShape = shape;
 }
 
 }  // namespace unapgpu

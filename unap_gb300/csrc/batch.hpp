@@ -9,7 +9,11 @@
 
 namespace unapgpu {
 
-constexpr int kBatchSmallCells = 65536;  // systems solved by one CTA each
+// Systems of at most team_solve_cells() cells (default below) are solved by
+// one fused launch, a team of CTAs per system (small_solve.cu).
+constexpr int kTeamSolveCells = 65536;
+int team_solve_cells();
+int set_team_solve_cells(int cells);  // returns the previous value; 0 turns it off
 
 struct BatchItem {
     Matrix* A = nullptr;
@@ -26,7 +30,7 @@ public:
     explicit BatchSolver(cudaStream_t s);
     ~BatchSolver();
     std::vector<SolveStats> solve(const std::vector<BatchItem>& items);
-    int lastThreads = 0;  // CTA size of the last fused launch
+    TeamShape lastShape{0, 0};  // shape of the last fused launch
 
     // drop the cached preconditioner diagonals of a matrix that is going away
     void forget(const Matrix* A);
@@ -54,10 +58,19 @@ private:
     const double* factor(Matrix& A, int precond);
     void solveSmall(const std::vector<BatchItem>& items, const std::vector<int>& idx,
                     std::vector<SolveStats>& out);
-    int autotune(int sizeClass, int m);
 };
 
-// CTA size the autotuner chose for a size class (0: not tuned yet)
-int batch_tuned_threads(int sizeClass);
+// Shape of a fused launch of m systems (device array d_systems, largest
+// nMax cells): the autotuner's choice for the pair (nMax rounded up to a
+// power of two, m in classes 1 / 2-4 / 5-16 / 17-64 / more).  The first
+// launch of a pair times every launchable shape (CTA size 128 .. 1024 x
+// cluster 1 .. 16 CTAs) on these systems with the iterations capped, the
+// initial guesses restored after each trial, and caches the fastest.
+TeamShape tuned_team_shape(cudaStream_t s, const SmallSystem* d_systems, int m, int nMax);
+// the cached shape of a pair ({0, 0}: not tuned yet)
+TeamShape cached_team_shape(int nMax, int m);
+// every later launch uses this shape instead of the tuner's (threads 0:
+// back to the tuner)
+void force_team_shape(int threads, int cluster);
 
 }  // namespace unapgpu

@@ -97,7 +97,32 @@ int unap_cuda_batch_solve(long int batch, int count, const unap_cuda_batch_item*
             stats[i].seconds = st[(size_t)i].seconds;
             stats[i].algorithmicBytes = st[(size_t)i].bytes;
         }
-        if (ctaThreads) *ctaThreads = h->S->lastThreads;
+        if (ctaThreads) *ctaThreads = h->S->lastShape.threads;
+    });
+}
+
+int unap_cuda_batch_last_shape(long int batch, int* ctaThreads, int* clusterCtas)
+{
+    return guarded([&] {
+        BatchHandle* h = batch_from(batch);
+        if (ctaThreads) *ctaThreads = h->S->lastShape.threads;
+        if (clusterCtas) *clusterCtas = h->S->lastShape.cluster;
+    });
+}
+
+int unap_cuda_set_team_solve_cells(int cells) { return set_team_solve_cells(cells); }
+
+int unap_cuda_force_team_shape(int ctaThreads, int clusterCtas)
+{
+    return guarded([&] { force_team_shape(ctaThreads, clusterCtas); });
+}
+
+int unap_cuda_team_shape(int cells, int systems, int* ctaThreads, int* clusterCtas)
+{
+    return guarded([&] {
+        const TeamShape t = cached_team_shape(cells, systems);
+        if (ctaThreads) *ctaThreads = t.threads;
+        if (clusterCtas) *clusterCtas = t.cluster;
     });
 }
 

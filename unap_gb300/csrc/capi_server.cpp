@@ -109,4 +109,6 @@ int unap_cuda_server_destroy(long int server)
     return guarded([&] { delete server_from(server); });
 }
 
+int unap_cuda_set_server_graphs(int on) { return set_server_graphs(on); }
+
 }  // extern "C"

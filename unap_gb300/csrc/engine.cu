@@ -2,13 +2,16 @@
 // drivers.  One solve keeps every vector and scalar on the device; the host
 // only enqueues gated iterations (captured once into a CUDA graph) and polls
 // the `done` flag of the device solver state between batches.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 
 #include "engine.hpp"
+#include "batch.hpp"
 
 namespace unapgpu {
 
@@ -23,6 +26,57 @@ bool& thread_in_capture()
 {
     static thread_local bool v = false;
     return v;
+}
+cudaStream_t& thread_alloc_stream()
+{
+    static thread_local cudaStream_t s = nullptr;
+    return s;
+}
+void keep_pool_memory()
+{
+    static std::mutex m;
+    static std::vector<int> done;
+    int dev = 0;
+    UNAP_CK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(m);
+    if (std::find(done.begin(), done.end(), dev) != done.end()) return;
+    cudaMemPool_t pool;
+    UNAP_CK(cudaDeviceGetDefaultMemPool(&pool, dev));
+    // freed blocks stay in the pool (up to 32 GiB) for the next allocations
+    unsigned long long keep = 32ull << 30;
+    UNAP_CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    done.push_back(dev);
+}
+namespace {
+std::mutex g_pinnedMutex;
+std::map<size_t, std::vector<void*>> g_pinnedFree;  // block size -> free blocks
+std::map<void*, size_t> g_pinnedSize;
+}  // namespace
+void* pinned_block_alloc(size_t bytes)
+{
+    const size_t sz = (bytes + 255) / 256 * 256;
+    {
+        std::lock_guard<std::mutex> lk(g_pinnedMutex);
+        auto& f = g_pinnedFree[sz];
+        if (!f.empty()) {
+            void* p = f.back();
+            f.pop_back();
+            return p;
+        }
+    }
+    void* p = nullptr;
+    UNAP_CK(gated_malloc_host(&p, sz));
+    std::lock_guard<std::mutex> lk(g_pinnedMutex);
+    g_pinnedSize[p] = sz;
+    return p;
+}
+void pinned_block_free(void* p)
+{
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(g_pinnedMutex);
+    auto it = g_pinnedSize.find(p);
+    if (it == g_pinnedSize.end()) return;
+    g_pinnedFree[it->second].push_back(p);
 }
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 const char* last_error() { return g_last_error.c_str(); }
@@ -84,6 +138,7 @@ public:
         *dotFused = true;
         return true;
     }
+    int lduType() const override { return 0; }
     int n;
 };
 
@@ -125,6 +180,8 @@ public:
         *dotFused = true;
         return true;
     }
+    int lduType() const override { return 1; }
+    const double* lduRD() const override { return rD.p; }
     int n;
     DevArray<double> rD;
 };
@@ -192,6 +249,8 @@ public:
         *dotFused = L.nWave > 0;
         return true;
     }
+    int lduType() const override { return dilu ? 3 : 2; }
+    const double* lduRD() const override { return rD.p; }
     const Level& L;
     bool dilu;
     DevArray<double> dfac, rD;
@@ -219,6 +278,7 @@ int set_default_executor(int persistent) { return g_persistent.exchange(persiste
 Krylov::Krylov(Matrix& A_, Precond* P_, Method m) : A(A_), P(P_), method(m)
 {
     useMega = g_persistent.load() != 0;
+    teamCells = team_solve_cells();
     n = A.n();
     ex.s = A.stream;
     ex.maxBlocks = device_max_blocks();
@@ -237,7 +297,7 @@ Krylov::Krylov(Matrix& A_, Precond* P_, Method m) : A(A_), P(P_), method(m)
         t.alloc(N);
     }
     UNAP_CK(gated_malloc((void**)&d_st, sizeof(KState)));
-    UNAP_CK(gated_malloc_host((void**)&h_st, sizeof(KState)));
+    h_st = static_cast<KState*>(pinned_block_alloc(sizeof(KState)));
     // partial buffers for one CTA per 256 rows (row kernels launch that many)
     pool.init(S_NSITES, std::max(ex.maxBlocks, div_up(n, kBlock)), std::max(1, A.L->nWave) + 1,
               ex.s);
@@ -250,7 +310,7 @@ Krylov::~Krylov()
     if (graphExec) cudaGraphExecDestroy(graphExec);
     if (graph) cudaGraphDestroy(graph);
     if (d_st) gated_free(d_st);
-    if (h_st) gated_free_host(h_st);
+    pinned_block_free(h_st);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
 }
@@ -457,8 +517,79 @@ void Krylov::runIterations()
     }
 }
 
+SolveStats Krylov::solveTeam(double* x_ref, const double* b_ref)
+{
+    // the whole solve in one launch: a team of CTAs (one, or a cluster)
+    // runs PCG.cpp:35-183 / PBiCGStab.cpp:45-459 with the preconditioner's
+    // own reciprocal diagonal; the launch shape comes from the autotuner
+    const Level& L = *A.L;
+    const size_t N = (size_t)n;
+    if (!teamWork.p) {
+        teamWork.alloc(N * (method == Method::PBiCGStab ? 8 : 3));
+        teamWaves.upload(L.waveStart, ex.s);
+        teamSys.alloc(sizeof(SmallSystem) + sizeof(SmallResult));
+    }
+    SmallSystem* dS = reinterpret_cast<SmallSystem*>(teamSys.p);
+    SmallResult* dR = reinterpret_cast<SmallResult*>(teamSys.p + sizeof(SmallSystem));
+    SmallSystem S{};
+    S.A = rows64(L);
+    S.waveStart = teamWaves.p;
+    S.nWave = L.nWave;
+    S.precond = P->lduType();
+    S.rD = S.precond ? P->lduRD() : nullptr;
+    S.method = method == Method::PBiCGStab ? 1 : 0;
+    S.tol = tol;
+    S.relTol = relTol;
+    S.maxIter = maxIter;
+    S.minIter = minIter;
+    S.zeroX = 0;
+    S.x = x.p;
+    S.b = b.p;
+    S.work = teamWork.p;
+    S.result = dR;
+    UNAP_CK(cudaMemcpyAsync(dS, &S, sizeof(S), cudaMemcpyHostToDevice, ex.s));
+    if (!cached_team_shape(n, 1).threads) {
+        // first solve of this size class: the tuner's trials run on this
+        // system (x restored after each), before the timed solve
+        k_to_internal<double>(ex, n, L.d_perm.p, x_ref, x.p);
+        k_to_internal<double>(ex, n, L.d_perm.p, b_ref, b.p);
+        (void)tuned_team_shape(ex.s, dS, 1, n);
+    }
+    const TeamShape shape = cached_team_shape(n, 1);
+    UNAP_CK(cudaEventRecord(ev0, ex.s));
+    k_to_internal<double>(ex, n, L.d_perm.p, x_ref, x.p);
+    k_to_internal<double>(ex, n, L.d_perm.p, b_ref, b.p);
+    launch_small_krylov(ex.s, dS, 1, nullptr, shape.threads, shape.cluster);
+    k_to_reference<double>(ex, n, L.d_perm.p, x.p, x_ref);
+    UNAP_CK(cudaEventRecord(ev1, ex.s));
+    SmallResult R{};
+    UNAP_CK(cudaMemcpyAsync(&R, dR, sizeof(R), cudaMemcpyDeviceToHost, ex.s));
+    UNAP_CK(cudaStreamSynchronize(ex.s));
+    UNAP_CK(cudaGetLastError());
+    SolveStats out;
+    float ms = 0;
+    UNAP_CK(cudaEventElapsedTime(&ms, ev0, ev1));
+    out.seconds = ms * 1e-3;
+    out.nIter = R.nIter;
+    out.initRes = R.initRes;
+    out.finalRes = R.finalRes;
+    out.converged = R.converged;
+    out.singular = R.singular;
+    if (!bytesKnown && method == Method::PCG) {
+        std::vector<Step> steps;
+        std::vector<LevelRows> lv;
+        int nInit = 0;
+        stepProgram(steps, lv, nInit);
+    }
+    if (bytesKnown) out.bytes = megaInitBytes + (double)out.nIter * megaIterBytes;
+    lastShape = shape;
+    return out;
+}
+
 SolveStats Krylov::solveDevice(double* x_ref, const double* b_ref)
 {
+    if (n > 0 && n <= teamCells && !flexible && !trueResidualRestart && P && P->lduType() >= 0)
+        return solveTeam(x_ref, b_ref);
     SolveStats out;
     const Level& L = *A.L;
     UNAP_CK(cudaEventRecord(ev0, ex.s));

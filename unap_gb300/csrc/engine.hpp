@@ -6,6 +6,7 @@
 
 #include "kernels.hpp"
 #include "mega.hpp"
+#include "small_solve.hpp"
 
 namespace unapgpu {
 
@@ -54,6 +55,10 @@ public:
         (void)out, (void)lv, (void)r, (void)w, (void)slot, (void)dotFused;
         return false;
     }
+    // LDU preconditioner type (0 none, 1 Diag, 2 DIC, 3 DILU; -1 other) and
+    // its reciprocal diagonal in internal order, for whole-solve launches
+    virtual int lduType() const { return -1; }
+    virtual const double* lduRD() const { return nullptr; }
 };
 
 std::unique_ptr<Precond> make_ldu_precond(int type, Matrix& A);  // 1 Diag, 2 DIC, 3 DILU, else none
@@ -71,6 +76,10 @@ public:
     bool trueResidualRestart = false;  // re-check ||b - Ax|| and restart if needed
     bool useGraph = true;
     bool useMega = true;     // PCG as one persistent cooperative launch when possible
+    // systems of at most this many cells with an LDU preconditioner (none,
+    // Diag, DIC, DILU) are solved by one whole-solve launch (small_solve.cu)
+    int teamCells = 0;
+    TeamShape lastShape{0, 0};  // shape of the last whole-solve launch
     // solve on device vectors in reference order (x in/out, b in)
     SolveStats solveDevice(double* x_ref, const double* b_ref);
     // solve on host vectors (copies in and out)
@@ -98,6 +107,10 @@ private:
     bool bytesKnown = false;
     // one PCG iteration (and the init part) as a step program; false for
     // methods or preconditioners without one
+    DevArray<double> teamWork;      // whole-solve launch: work vectors
+    DevArray<int> teamWaves;        // and wavefront ranges
+    DevArray<unsigned char> teamSys;  // its SmallSystem and SmallResult
+    SolveStats solveTeam(double* x_ref, const double* b_ref);
     bool stepProgram(std::vector<Step>& steps, std::vector<LevelRows>& lv, int& nInit);
     bool buildMega();
     void enqueueIteration();

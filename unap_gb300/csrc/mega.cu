@@ -507,13 +507,13 @@ bool mega_single_level(int nRows) { return nRows <= 48 * 1024; }
 
 MegaRunner::MegaRunner()
 {
-    UNAP_CK(gated_malloc_host((void**)&h_status, sizeof(MegaStatus)));
+    h_status = static_cast<MegaStatus*>(pinned_block_alloc(sizeof(MegaStatus)));
     d_status.alloc(1);
 }
 
 MegaRunner::~MegaRunner()
 {
-    if (h_status) gated_free_host(h_status);
+    pinned_block_free(h_status);
 }
 
 int MegaRunner::threads() const { return kMegaThreads; }

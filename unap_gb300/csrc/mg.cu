@@ -219,7 +219,7 @@ MgSolver::MgSolver(Matrix& A_, const std::vector<double>& weights, const MgParam
     eig.alloc((size_t)nC + 1);
     chebyFirst.assign((size_t)nC + 1, 1);
     UNAP_CK(gated_malloc((void**)&d_st, sizeof(KState)));
-    UNAP_CK(gated_malloc_host((void**)&h_st, sizeof(KState)));
+    h_st = static_cast<KState*>(pinned_block_alloc(sizeof(KState)));
     pool.init(M_NSITES, ex.maxBlocks, 2, s);
     UNAP_CK(cudaEventCreate(&ev0));
     UNAP_CK(cudaEventCreate(&ev1));
@@ -229,7 +229,7 @@ MgSolver::MgSolver(Matrix& A_, const std::vector<double>& weights, const MgParam
 MgSolver::~MgSolver()
 {
     if (d_st) gated_free(d_st);
-    if (h_st) gated_free_host(h_st);
+    pinned_block_free(h_st);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
 }

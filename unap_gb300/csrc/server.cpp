@@ -6,6 +6,14 @@
 
 namespace unapgpu {
 
+namespace {
+std::atomic<int> g_serverGraphs{1};
+}  // namespace
+
+int server_graphs() { return g_serverGraphs.load(); }
+int set_server_graphs(int on) { return g_serverGraphs.exchange(on ? 1 : 0); }
+
+
 double now_seconds()
 {
     using namespace std::chrono;
@@ -117,6 +125,10 @@ void Server::largeWorker()
 {
     cudaStream_t s = nullptr;
     cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    // every device array of this slot's requests comes from the memory pool
+    // in this stream's order: a slot's setup never synchronizes the device
+    // (and so never waits for the other slots' solves)
+    StreamAllocScope scope(s);
     for (;;) {
         ServeRequest* r = nullptr;
         {
@@ -171,11 +183,12 @@ void Server::largeWorker()
             K.flexible = flexible;
             K.trueResidualRestart = restart;
             // concurrent slots share the SMs: the persistent cooperative
-            // executor needs every SM, so slots launch their steps directly.
-            // (Graph replay was measured slower here: each capture holds
-            // the capture gate against the other slots' setup allocations.)
+            // executor needs every SM, so slots run per-step kernels,
+            // replayed from CUDA graphs.  The slot's allocations are
+            // stream-ordered, so a capture never meets another slot's
+            // device-synchronizing allocation.
             K.useMega = params.maxSlots == 1;
-            K.useGraph = false;
+            K.useGraph = server_graphs() != 0;
             r->tSetup = now_seconds();
             r->st = K.solveDevice(dx.p, db.p);
             r->x.resize(n);
@@ -195,6 +208,7 @@ void Server::batchWorker()
     cudaStream_t s = nullptr;
     cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     {
+        StreamAllocScope scope(s);
         BatchSolver B(s);
         for (;;) {
             std::vector<ServeRequest*> take;

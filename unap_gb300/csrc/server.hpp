@@ -38,6 +38,11 @@ struct ServeRequest {
     bool done = false;
 };
 
+// Slots replay each Krylov iteration from a CUDA graph (1, default) or
+// launch its kernels one by one (0); returns the previous setting.
+int server_graphs();
+int set_server_graphs(int on);
+
 struct ServerParams {
     long long memoryBudget = 0;  // bytes; 0: 80% of free device memory at start
     int maxSlots = 4;            // concurrent large solves (one stream each)

@@ -7,6 +7,12 @@ namespace unapgpu {
 
 constexpr int kSmallBlock = 512;
 
+// Launch shape of a fused solve: CTA size and CTAs per system.
+struct TeamShape {
+    int threads = kSmallBlock;
+    int cluster = 1;
+};
+
 struct SmallResult {
     int nIter, converged, singular, pad;
     double initRes, finalRes;
@@ -28,9 +34,16 @@ struct SmallSystem {
     SmallResult* result;        // may be null
 };
 
-// One block of `threads` (128, 256, 512 or 1024) per system; skipped when
-// gate->done is set.
+// A team of `cluster` CTAs (1, 2, 4, 8 or 16; a thread-block cluster when
+// above 1) of `threads` threads (128, 256, 512 or 1024) per system; skipped
+// when gate->done is set.
 void launch_small_krylov(cudaStream_t s, const SmallSystem* d_systems, int count,
-                         const KState* gate, int threads = kSmallBlock);
+                         const KState* gate, int threads = kSmallBlock, int cluster = 1);
+
+bool small_team_size_ok(int threads, int cluster);
+
+// Teams of this shape resident at once on the current device (0: the shape
+// cannot be launched there).
+int small_team_capacity(int threads, int cluster);
 
 }  // namespace unapgpu

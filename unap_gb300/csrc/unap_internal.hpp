@@ -93,23 +93,60 @@ inline cudaError_t gated_free_host(void* p)
     return cudaFreeHost(p);
 }
 
+// Stream-ordered allocation scope.  While a thread holds one, the DevArrays
+// it allocates come from the device's memory pool in the order of the
+// scope's stream (cudaMallocAsync) and return to the pool in that order when
+// released (cudaFreeAsync): no device-wide synchronization and no allocation
+// gate, so concurrent solves on other streams keep running.  Everything
+// that touches those arrays must run on the scope's stream (the server's
+// slot workers: one stream each).  The pool keeps freed memory for reuse
+// instead of returning it to the driver at each synchronization.
+cudaStream_t& thread_alloc_stream();
+void keep_pool_memory();
+struct StreamAllocScope {
+    cudaStream_t prev;
+    explicit StreamAllocScope(cudaStream_t s) : prev(thread_alloc_stream())
+    {
+        keep_pool_memory();
+        thread_alloc_stream() = s;
+    }
+    ~StreamAllocScope() { thread_alloc_stream() = prev; }
+    StreamAllocScope(const StreamAllocScope&) = delete;
+    StreamAllocScope& operator=(const StreamAllocScope&) = delete;
+};
+
+// Small pinned host blocks (solver state read back every iteration) from a
+// process-wide free list: cudaFreeHost would synchronize the device.
+void* pinned_block_alloc(size_t bytes);
+void pinned_block_free(void* p);
+
 template <class T>
 struct DevArray {
     T* p = nullptr;
     size_t n = 0;
+    cudaStream_t as = nullptr;  // allocation stream of a stream-ordered array
+    bool async = false;
     DevArray() = default;
     explicit DevArray(size_t count) { alloc(count); }
     DevArray(const DevArray&) = delete;
     DevArray& operator=(const DevArray&) = delete;
-    DevArray(DevArray&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevArray(DevArray&& o) noexcept : p(o.p), n(o.n), as(o.as), async(o.async)
+    {
+        o.p = nullptr;
+        o.n = 0;
+        o.async = false;
+    }
     DevArray& operator=(DevArray&& o) noexcept
     {
         if (this != &o) {
             release();
             p = o.p;
             n = o.n;
+            as = o.as;
+            async = o.async;
             o.p = nullptr;
             o.n = 0;
+            o.async = false;
         }
         return *this;
     }
@@ -118,23 +155,42 @@ struct DevArray {
     {
         release();
         n = count;
-        if (count) UNAP_CK(gated_malloc((void**)&p, count * sizeof(T)));
+        if (!count) return;
+        cudaStream_t s = thread_alloc_stream();
+        if (s) {
+            if (thread_in_capture())
+                throw std::logic_error("device allocation inside a stream capture");
+            UNAP_CK(cudaMallocAsync((void**)&p, count * sizeof(T), s));
+            as = s;
+            async = true;
+        } else {
+            UNAP_CK(gated_malloc((void**)&p, count * sizeof(T)));
+        }
     }
     void release()
     {
-        if (p) gated_free(p);
+        if (p) {
+            if (async)
+                cudaFreeAsync(p, as);
+            else
+                gated_free(p);
+        }
         p = nullptr;
         n = 0;
+        async = false;
     }
+    // stream 0 means the array's own stream for a stream-ordered array
+    cudaStream_t on(cudaStream_t s) const { return (!s && async) ? as : s; }
     void upload(const T* h, size_t count, cudaStream_t s = 0)
     {
         if (count != n) alloc(count);
-        if (count) UNAP_CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+        if (count)
+            UNAP_CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, on(s)));
     }
     void upload(const std::vector<T>& h, cudaStream_t s = 0) { upload(h.data(), h.size(), s); }
     void zero(cudaStream_t s = 0)
     {
-        if (n) UNAP_CK(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+        if (n) UNAP_CK(cudaMemsetAsync(p, 0, n * sizeof(T), on(s)));
     }
     size_t bytes() const { return n * sizeof(T); }
 };
