@@ -433,7 +433,7 @@ class _Builder:
 
 
 def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 12, compare_plain: bool = True,
-                window: int = 64, procs: int = 0):
+                window: int = 64, procs: int = 0, prebuild: bool = False):
     """Config c5 served: the seeded request stream (Poisson arrivals at 200/s,
     sizes log-uniform 8k-2M cells, 60% mixed AMG-PCG / 25% PCG+DIC / 15%
     PBiCGStab+DILU, tol 1e-8) submitted on its arrival schedule to the
@@ -451,7 +451,13 @@ def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 12, compare_pla
     specs = W.serving_stream(count=n_requests, rate=200.0, seed=seed)
     procs = procs or max(2, min(12, (os.cpu_count() or 4) - 4))
     srv = capi.Server(max_slots=max_slots)
-    B = _Builder(specs, window, procs)
+    B = _Builder(specs, len(specs) if prebuild else window, procs)
+    if prebuild:
+        # every request built before the first arrival: the builders'
+        # processes are idle while the server runs
+        built = [B.get(i) for i in range(len(specs))]
+        B.close()
+        B = None
     sub_t, ids, ns, inflight_at_late = [], [], [], []
     results = [None] * len(specs)
     done_count = [0]
@@ -472,7 +478,11 @@ def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 12, compare_pla
     th.start()
     t0 = time.perf_counter()
     for i, sp in enumerate(specs):
-        r = B.get(i)
+        if B is None:
+            r = built[i]
+            built[i] = None
+        else:
+            r = B.get(i)
         with lock:  # bounded server queue: at most `window` requests in flight
             lock.wait_for(lambda: len(ids) - done_count[0] < window)
         dt = sp.arrival - (time.perf_counter() - t0)
@@ -490,7 +500,8 @@ def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 12, compare_pla
         del r
     th.join()
     srv.close()
-    B.close()
+    if B is not None:
+        B.close()
     lat, setup, solve_t, queue, batched = [], [], [], [], 0
     for sp, st_, info in zip(specs, sub_t, results):
         if not info["converged"]:

@@ -437,6 +437,11 @@ int unap_cuda_server_destroy(long int server);
  * default) or launch its kernels one by one (0); applies to requests started
  * afterwards; returns the previous setting */
 int unap_cuda_set_server_graphs(int on);
+/* PCG/PBiCGStab requests of up to `cells` cells that a server slot solves
+ * (those above the batch lane's size) run as one whole-solve launch on a
+ * thread-block cluster (default: every size; 0: per-step launches);
+ * returns the previous value */
+int unap_cuda_set_server_team_cells(int cells);
 
 int unap_cuda_device_synchronize(void);
 
@@ -458,6 +463,13 @@ long long unap_cuda_launch_count(void);
  * program.  Both give the same iterates up to dot-product summation order.
  * Returns the previous setting.  No counterpart in the reference. */
 int unap_cuda_set_executor(int persistent);
+
+/* How host threads of this process wait for the GPU (synchronizations,
+ * read-backs) on the current device: 0 the CUDA default, 1 spin, 2 yield,
+ * 3 block on an OS primitive (frees the core for other host threads, e.g.
+ * a server's slot workers).  Call before the device's context is created
+ * (the first CUDA call of the process on that device). */
+int unap_cuda_set_host_wait(int mode);
 
 /* Per-wavefront Gauss-Seidel launches use programmatic dependent launch:
  * the next wavefront's kernel starts launching while the previous one runs

@@ -120,6 +120,7 @@ SIGNATURES = {
     "unap_cuda_amg_destroy": (_c_int, [_c_long]),
     "unap_cuda_launch_count": (_c_ll, []),
     "unap_cuda_set_executor": (_c_int, [_c_int]),
+    "unap_cuda_set_host_wait": (_c_int, [_c_int]),
     "unap_cuda_set_wave_pdl": (_c_int, [_c_int]),
     "unap_cuda_set_wave_grid": (_c_int, [_c_int]),
     "unap_cuda_set_packed_sweeps": (_c_int, [_c_int]),
@@ -151,6 +152,7 @@ SIGNATURES = {
     "unap_cuda_team_shape": (_c_int, [_c_int, _c_int, _ip, _ip]),
     "unap_cuda_force_team_shape": (_c_int, [_c_int, _c_int]),
     "unap_cuda_set_server_graphs": (_c_int, [_c_int]),
+    "unap_cuda_set_server_team_cells": (_c_int, [_c_int]),
     "unap_cuda_server_create": (_c_int, [_lp, _c_ll, _c_int, _c_int]),
     "unap_cuda_server_submit": (_c_int, [_c_long, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp,
                                          _c_int, _c_dbl, _c_int, ctypes.POINTER(_c_ll)]),
@@ -317,6 +319,12 @@ def set_executor(persistent: bool) -> bool:
     return bool(load().unap_cuda_set_executor(1 if persistent else 0))
 
 
+def set_host_wait(mode: int) -> None:
+    """How host threads wait for the GPU: 0 default, 1 spin, 2 yield, 3
+    blocking; call before the first CUDA work of the process."""
+    check(load().unap_cuda_set_host_wait(int(mode)))
+
+
 def set_team_solve_cells(cells: int) -> int:
     """Systems of at most `cells` cells with an LDU preconditioner are solved
     by one whole-solve launch (0: never); returns the previous value."""
@@ -327,6 +335,12 @@ def set_server_graphs(on: bool) -> bool:
     """Server slots replay Krylov iterations from CUDA graphs (default) or
     launch kernel by kernel; returns the previous setting."""
     return bool(load().unap_cuda_set_server_graphs(1 if on else 0))
+
+
+def set_server_team_cells(cells: int) -> int:
+    """Server slots solve PCG/PBiCGStab requests of up to `cells` cells in
+    one whole-solve launch (0: never); returns the previous value."""
+    return int(load().unap_cuda_set_server_team_cells(int(cells)))
 
 
 def force_team_shape(threads: int, cluster: int = 1) -> None:

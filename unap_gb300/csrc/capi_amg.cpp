@@ -237,6 +237,18 @@ long long unap_cuda_launch_count(void) { return launch_count(); }
 
 int unap_cuda_set_executor(int persistent) { return set_default_executor(persistent); }
 
+int unap_cuda_set_host_wait(int mode)
+{
+    return guarded([&] {
+        unsigned flags = mode == 1   ? cudaDeviceScheduleSpin
+                         : mode == 2 ? cudaDeviceScheduleYield
+                         : mode == 3 ? cudaDeviceScheduleBlockingSync
+                                     : cudaDeviceScheduleAuto;
+        if (mode < 0 || mode > 3) throw std::invalid_argument("host wait mode must be 0 to 3");
+        UNAP_CK(cudaSetDeviceFlags(flags));
+    });
+}
+
 int unap_cuda_set_wave_pdl(int on) { return set_wave_pdl(on); }
 
 int unap_cuda_set_wave_grid(int oneRowPerThread) { return set_wave_grid(oneRowPerThread); }

@@ -111,4 +111,6 @@ int unap_cuda_server_destroy(long int server)
 
 int unap_cuda_set_server_graphs(int on) { return set_server_graphs(on); }
 
+int unap_cuda_set_server_team_cells(int cells) { return set_server_team_cells(cells); }
+
 }  // extern "C"

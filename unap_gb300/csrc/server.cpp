@@ -1,4 +1,5 @@
 // Continuous-batching solve server (see server.hpp).
+#include <algorithm>
 #include <chrono>
 
 #include "amg.hpp"
@@ -8,10 +9,12 @@ namespace unapgpu {
 
 namespace {
 std::atomic<int> g_serverGraphs{1};
+std::atomic<int> g_serverTeamCells{1 << 30};
 }  // namespace
 
 int server_graphs() { return g_serverGraphs.load(); }
 int set_server_graphs(int on) { return g_serverGraphs.exchange(on ? 1 : 0); }
+int set_server_team_cells(int cells) { return g_serverTeamCells.exchange(std::max(cells, 0)); }
 
 
 double now_seconds()
@@ -189,6 +192,11 @@ void Server::largeWorker()
             // device-synchronizing allocation.
             K.useMega = params.maxSlots == 1;
             K.useGraph = server_graphs() != 0;
+            // a PCG/PBiCGStab request runs as one whole-solve launch on a
+            // thread-block cluster: it holds a few SMs for the whole solve
+            // instead of issuing tens of thousands of wavefront launches
+            // that contend with the other slots' launches
+            K.teamCells = g_serverTeamCells.load();
             r->tSetup = now_seconds();
             r->st = K.solveDevice(dx.p, db.p);
             r->x.resize(n);

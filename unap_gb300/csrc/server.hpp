@@ -42,6 +42,10 @@ struct ServeRequest {
 // launch its kernels one by one (0); returns the previous setting.
 int server_graphs();
 int set_server_graphs(int on);
+// PCG/PBiCGStab requests of up to this many cells that a slot (not the
+// batch lane) solves run as one whole-solve launch (default: all; 0: never);
+// returns the previous value.
+int set_server_team_cells(int cells);
 
 struct ServerParams {
     long long memoryBudget = 0;  // bytes; 0: 80% of free device memory at start
