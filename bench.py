@@ -69,6 +69,16 @@ CONFIGS = {
                kind="krylov", method=1, precond=3, rel_tol=1e-9),
 }
 L2_BYTES = 129 * 2 ** 20
+# DRAM bytes (read + write) per algorithmic byte of a kernel family, from
+# one ncu capture of a smaller case; the roofline's `traffic` scales it to
+# the launch group's algorithmic bytes (the traffic grows with the rows)
+TRAFFIC_RATIO = {
+    "cheb_step_kernel<float>": (
+        327.9 / 258.9,
+        "ncu dram__bytes_read.sum + dram__bytes_write.sum of one Chebyshev step on level 1 "
+        "of the 192^3 hierarchy (3,273,854 rows): 327.9 MB against 258.9 MB algorithmic, "
+        "scaled by the launch group's algorithmic bytes"),
+}
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -892,8 +902,11 @@ def main():
                  "achieved": solve_bytes / statistics.mean(dev_s) / 1e9}
         whole["frac"] = whole["achieved"] / peak
     tg = groups[top]
+    ratio = TRAFFIC_RATIO.get(tg["kernel"])
     roofline = {"bound": "hbm", "achieved": tg["achieved"], "peak": peak, "unit": "GB/s",
-                "frac": tg["achieved"] / peak, "traffic": None,
+                "frac": tg["achieved"] / peak,
+                "traffic": ratio[0] * tg["algorithmic_bytes_per_vcycle"] if ratio else None,
+                "traffic_basis": ratio[1] if ratio else None,
                 "kernel": tg["kernel"], "levels": tg["levels"],
                 "launch_group": ("every launch of this kernel in one V-cycle, each level's "
                                  "launch group timed alone with CUDA events on the matrix's "

@@ -344,6 +344,11 @@ int unap_cuda_amg_profile_smoother(long int amg, int level, int reps, double* ms
  * coarsest (0 on Gauss-Seidel levels): lam[k] for k < min(nLevels - 1,
  * maxOut); *written = entries filled.  No counterpart in the reference. */
 int unap_cuda_amg_eigenvalues(long int amg, double* lam, int maxOut, int* written);
+/* Host wall time of the hierarchy's setup phases, seconds[0..5]: face
+ * weights and agglomeration; coarse level builds and transfer maps; the
+ * coarsest inverse; level vectors and FP32 copies; row packing; eigenvalue
+ * estimates.  No counterpart in the reference. */
+int unap_cuda_amg_setup_phases(long int amg, double* seconds);
 /* AMG-PCG on device vectors (x holds the initial guess) */
 int unap_cuda_amg_solve(long int amg, double* x, const double* b, unap_cuda_stats* stats);
 /* AMG-PCG on host vectors: copies b and x in, solves, copies x out */
@@ -509,9 +514,9 @@ int unap_cuda_set_cheby_small_rows(int rows);
  * counterpart in the reference. */
 int unap_cuda_set_matrix_wavefronts(int on);
 /* Entries of a row the Chebyshev step loads per dependent round trip: 0
- * (default) 16 on levels averaging more than 8 entries per row and 8
- * elsewhere, or 8 / 16 everywhere (fewer registers and more resident warps
- * against one round trip per row).  Results are identical.  Returns the
+ * (default) 16 on levels averaging more than 8 entries per row, except FP32
+ * levels of 2^20 rows or more, and 8 elsewhere; or 8 / 16 everywhere (fewer
+ * registers and more resident warps against one round trip per row).  Results are identical.  Returns the
  * previous setting, or UNAP_CUDA_EINVAL for another value.  No counterpart
  * in the reference. */
 int unap_cuda_set_cheby_chunk(int entries);

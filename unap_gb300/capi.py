@@ -109,6 +109,7 @@ SIGNATURES = {
     "unap_cuda_amg_info": (_c_int, [_c_long, _ip, _vp, _vp, _c_int, _dp,
                                     ctypes.POINTER(_c_ll)]),
     "unap_cuda_amg_vcycle": (_c_int, [_c_long, _vp, _vp]),
+    "unap_cuda_amg_setup_phases": (_c_int, [_c_long, _vp]),
     "unap_cuda_amg_eigenvalues": (_c_int, [_c_long, _vp, _c_int, _vp]),
     "unap_cuda_amg_profile_smoother": (_c_int, [_c_long, _c_int, _c_int, _vp, _vp, _vp]),
     "unap_cuda_set_cheby_small_rows": (_c_int, [_c_int]),
@@ -526,6 +527,14 @@ class DeviceAmg:
         check(load().unap_cuda_amg_profile_smoother(self.handle, level, reps, ctypes.byref(ms),
                                                     ctypes.byref(b), ctypes.byref(n)))
         return ms.value, b.value, n.value
+
+    def setup_phases(self):
+        """Host wall time (s) of the setup phases: agglomeration, levels,
+        coarsest, vectors, packing, eigenvalues."""
+        t = np.zeros(6)
+        check(load().unap_cuda_amg_setup_phases(self.handle, t.ctypes.data))
+        return dict(zip(["agglomerate", "levels", "coarsest", "vectors", "pack", "eigen"],
+                        t.tolist()))
 
     def eigenvalues(self):
         """Chebyshev eigenvalue estimate of every level but the coarsest

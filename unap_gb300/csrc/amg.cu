@@ -50,9 +50,16 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
             "AMG Gauss-Seidel smoothing needs oriented, owner-sorted faces and a matrix built "
             "with wavefronts");
     cudaStream_t s = A.stream;
+    auto tp = t0;
+    auto phase = [&](int i) {
+        const auto t = std::chrono::steady_clock::now();
+        setupPhase[i] = std::chrono::duration<double>(t - tp).count();
+        tp = t;
+    };
     std::vector<double> w = mg_face_weights(A.host);
     std::vector<CoarseHost> coarse =
         agglomerate_levels(A.host, w, params.nCoarsest, params.maxLevels, 1, s);
+    phase(0);
     const int L = (int)coarse.size();
     lv.resize((size_t)L + 1);
     lv[0].L = A.L.get();
@@ -98,6 +105,7 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
         lv[(size_t)k].cmap.upload(cmap, s);
         UNAP_CK(cudaStreamSynchronize(s));
     }
+    phase(1);
     // coarsest: dense FP64 inverse (identity internal order when L >= 1)
     const HostLdu& Ch = L ? coarse[(size_t)L - 1].A : A.host;
     nc = Ch.n;
@@ -132,6 +140,7 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
             Minv.upload(cm, s);
         }
     }
+    phase(2);
     {
         std::vector<int> all;
         waveOff.assign((size_t)L + 2, 0);
@@ -158,6 +167,7 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
         }
     }
     UNAP_CK(cudaStreamSynchronize(s));
+    phase(3);
     // row-packed copies of the levels the cluster tail may run (in the
     // precision of the V-cycle)
     for (int k = 0; k < L; ++k) {
@@ -167,8 +177,11 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
         else
             pack_rows<double>(rows64(*lv[(size_t)k].L), lv[(size_t)k].pack, s);
     }
+    UNAP_CK(cudaStreamSynchronize(s));
+    phase(4);
     if (params.smoother == 1) setupCheby(s);
     tail_cluster_size();  // function attributes and the cluster query, outside any capture
+    phase(5);
     setupSeconds =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }

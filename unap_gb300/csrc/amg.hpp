@@ -80,6 +80,10 @@ public:
                       double* z);
     AmgParams params;
     double setupSeconds = 0;
+    // host wall time of the setup phases, seconds: face weights and
+    // agglomeration, coarse level builds and transfer maps, coarsest
+    // inverse, vectors and FP32 copies, row packing, eigenvalue estimates
+    double setupPhase[6] = {0, 0, 0, 0, 0, 0};
     size_t deviceBytes() const;
 
     struct Lv {

@@ -191,6 +191,15 @@ int unap_cuda_amg_profile_smoother(long int amg, int level, int reps, double* ms
     });
 }
 
+int unap_cuda_amg_setup_phases(long int amg, double* seconds)
+{
+    return guarded([&] {
+        AmgHandle* h = amg_from(amg);
+        for (int i = 0; i < 6; ++i)
+            if (seconds) seconds[i] = h->H->setupPhase[i];
+    });
+}
+
 int unap_cuda_amg_eigenvalues(long int amg, double* lam, int maxOut, int* written)
 {
     return guarded([&] {

@@ -17,7 +17,12 @@ void tick()
 }
 
 std::atomic<int> g_smallRows{100000};
-std::atomic<int> g_chunk{0};  // 0: 16 entries on long-row levels, else 8
+// 0: 16 entries on long-row levels below kChunk8Rows rows, else 8.  Large
+// FP32 levels are bandwidth-bound and the 8-entry form holds six CTAs per
+// SM instead of four (256^3 hierarchy, level 1: 163 vs 179 us per step);
+// small ones are latency-bound and want one round trip per row.
+std::atomic<int> g_chunk{0};
+constexpr int kChunk8Rows = 1 << 20;
 
 // ---- eigenDiagPCG::diagPCGLoops (eigenDiagPCG.cpp:48-238) ----------------
 __global__ void __launch_bounds__(kBlock) eig_wr_kernel(int n, const double* __restrict__ rD,
@@ -161,8 +166,11 @@ __global__ void recip_kernel(int n, const double* __restrict__ d, double* __rest
         r[i] = 1.0 / d[i];
 }
 
+// FP32 steps with 8-entry chunks fit 40 registers: six CTAs per SM (48
+// warps) keep more row loads in flight than the 16-entry form's four
 template <class T, int CK>
-__global__ void __launch_bounds__(kBlock) cheb_step_kernel(Rows<T> A, const T* xin, T* xout,
+__global__ void __launch_bounds__(kBlock, (CK == 8 && sizeof(T) == 4) ? 6 : 1)
+    cheb_step_kernel(Rows<T> A, const T* xin, T* xout,
                                                            const T* __restrict__ b, T* w, T c1,
                                                            T c2, int first, Gate g)
 {
@@ -358,7 +366,7 @@ void k_cheb_step(const Exec& ex, const Rows<T>& A, const T* xin, T* xout, const 
     cfg.numAttrs = wave_pdl() ? 1 : 0;
     tick();
     const int ck = g_chunk.load();
-    if (ck == 16 || (ck == 0 && A.wide))
+    if (ck == 16 || (ck == 0 && A.wide && (sizeof(T) == 8 || A.n < kChunk8Rows)))
         UNAP_CK(cudaLaunchKernelEx(&cfg, cheb_step_kernel<T, 16>, A, xin, xout, b, w, c1, c2,
                                    first, g));
     else

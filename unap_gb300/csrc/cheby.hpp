@@ -78,8 +78,9 @@ void k_prolong_add_to(const Exec& ex, int n, const int* cmap, const T* coarse, c
 // (spread over more SMs); returns the previous value.
 int set_cheby_small_rows(int rows);
 // Entries of a row loaded per dependent round trip by the Chebyshev step: 0
-// (default) 16 on levels averaging more than 8 entries per row, else 8; 8 or
-// 16 on every level.  Returns the previous value.
+// (default) 16 on levels averaging more than 8 entries per row, except FP32
+// levels of a million rows or more (8: more CTAs per SM), else 8; 8 or 16
+// on every level.  Returns the previous value.
 int set_cheby_chunk(int entries);
 
 }  // namespace unapgpu

@@ -9,7 +9,7 @@ namespace unapgpu {
 
 namespace {
 std::atomic<int> g_serverGraphs{1};
-std::atomic<int> g_serverTeamCells{1 << 30};
+std::atomic<int> g_serverTeamCells{0};
 }  // namespace
 
 int server_graphs() { return g_serverGraphs.load(); }
