@@ -310,6 +310,10 @@ typedef struct {
     int chebyDegree; /* default 3 (1..16) */
     int chebyFrom;   /* first Chebyshev level, default 0 (all) */
     double eigRatio; /* default 30 */
+    int fusedOuter;  /* 1 (default): with an FP32 V-cycle, the outer PCG's
+                        SpMV, dots and updates use fused multiply-adds (half
+                        the FP64 instructions; GB300's FP64 pipe bounds them);
+                        0: the reference's separate roundings */
 } unap_cuda_amg_params;
 
 void unap_cuda_amg_default_params(unap_cuda_amg_params* p);

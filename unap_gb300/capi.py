@@ -467,7 +467,7 @@ class AmgParams(ctypes.Structure):
                 ("nPostSweeps", _c_int), ("precision", _c_int), ("flexible", _c_int),
                 ("tol", _c_dbl), ("relTol", _c_dbl), ("maxIter", _c_int), ("minIter", _c_int),
                 ("smoother", _c_int), ("chebyDegree", _c_int), ("chebyFrom", _c_int),
-                ("eigRatio", _c_dbl)]
+                ("eigRatio", _c_dbl), ("fusedOuter", _c_int)]
 
 
 class DeviceAmg:
@@ -483,7 +483,7 @@ class DeviceAmg:
                      n_post="nPostSweeps", precision="precision", flexible="flexible",
                      tol="tol", rel_tol="relTol", max_iter="maxIter", min_iter="minIter",
                      smoother="smoother", cheby_degree="chebyDegree", cheby_from="chebyFrom",
-                     eig_ratio="eigRatio")
+                     eig_ratio="eigRatio", fused_outer="fusedOuter")
         for k, v in kw.items():
             setattr(self.params, names[k], v)
         h = _c_long(0)

@@ -86,6 +86,7 @@ void unap_cuda_amg_default_params(unap_cuda_amg_params* p)
     p->chebyDegree = 3;
     p->chebyFrom = 0;
     p->eigRatio = 30.0;
+    p->fusedOuter = 1;
 }
 
 int unap_cuda_amg_create(long int* amg, long int matrix, const unap_cuda_amg_params* p)
@@ -118,6 +119,7 @@ int unap_cuda_amg_create(long int* amg, long int matrix, const unap_cuda_amg_par
         h->K->maxIter = h->p.maxIter;
         h->K->minIter = h->p.minIter;
         h->K->flexible = h->p.flexible != 0;
+        h->K->fusedOuter = h->p.precision == 1 && h->p.fusedOuter != 0;
         h->K->trueResidualRestart = true;
         *amg = reinterpret_cast<long int>(h.release());
     });

@@ -141,14 +141,22 @@ __device__ __forceinline__ T lds(const T* p)
 // Entries are processed in chunks of CK: all index/value loads of a chunk
 // are issued, then all gathers, then the in-order accumulation, so a row of
 // up to CK entries costs two dependent memory round trips.
-template <class T, int XL = XL_NC, bool ST = false, int CK = 8>
+//
+// FM: each product-and-sum as one fused multiply-add (one rounding), for
+// the mixed-precision solve's FP64 outer loop, where GB300's FP64 pipe and
+// not the bytes bounds the SpMV; FM = false keeps the reference's separate
+// roundings.
+template <class T, int XL = XL_NC, bool ST = false, int CK = 8, bool FM = false>
 __device__ __forceinline__ T row_apply(const Rows<T>& A, int r, const T* x)
 {
     const int info = lds<ST>(A.rowInfo + r);
     const int len = info & 0xffff;
     const int base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
     T acc = T(0);
-    acc += lds<ST>(A.diag + r) * ldx<XL>(x + r);
+    if constexpr (FM)
+        acc = lds<ST>(A.diag + r) * ldx<XL>(x + r);
+    else
+        acc += lds<ST>(A.diag + r) * ldx<XL>(x + r);
     for (int j0 = 0; j0 < len; j0 += CK) {
         int c[CK];
         T v[CK], xv[CK];
@@ -162,7 +170,12 @@ __device__ __forceinline__ T row_apply(const Rows<T>& A, int r, const T* x)
         for (int k = 0; k < CK; ++k) xv[k] = ldx<XL>(x + c[k]);
 #pragma unroll
         for (int k = 0; k < CK; ++k)
-            if (j0 + k < len) acc += v[k] * xv[k];
+            if (j0 + k < len) {
+                if constexpr (FM)
+                    acc = fma(v[k], xv[k], acc);
+                else
+                    acc += v[k] * xv[k];
+            }
     }
     return acc;
 }

@@ -349,11 +349,11 @@ void Krylov::enqueuePcgIteration()
     } else {
         P->apply(ex, r.p, z.p, nullptr, 0, d_st, FIN_NONE, g);
         k_dot2(ex, n, z.p, r.p, flexible ? z.p : nullptr, flexible ? q.p : nullptr,
-               pool.site(S_WR, d_st, FIN_PCG_WR), g);
+               pool.site(S_WR, d_st, FIN_PCG_WR), g, fusedOuter);
     }
-    k_pcg_direction(ex, n, z.p, p.p, d_st, g);
-    k_spmv<double>(ex, Ar, p.p, q.p, p.p, pool.site(S_ALPHA, d_st, FIN_PCG_ALPHA), g);
-    k_pcg_update(ex, n, x.p, r.p, p.p, q.p, pool.site(S_RES, d_st, FIN_PCG_RES), g);
+    k_pcg_direction(ex, n, z.p, p.p, d_st, g, fusedOuter);
+    k_spmv<double>(ex, Ar, p.p, q.p, p.p, pool.site(S_ALPHA, d_st, FIN_PCG_ALPHA), g, fusedOuter);
+    k_pcg_update(ex, n, x.p, r.p, p.p, q.p, pool.site(S_RES, d_st, FIN_PCG_RES), g, fusedOuter);
 }
 
 // PBiCGStab.cpp:155-456.  rA0.rA of the next iteration is fused into the

@@ -73,6 +73,9 @@ public:
     double tol = 0.0, relTol = 1e-6;
     int maxIter = 1000, minIter = 0;
     bool flexible = false;   // PCG only
+    // PCG's outer vector work (SpMV, dots, updates) in fused multiply-adds:
+    // half the FP64 instructions (the mixed-precision AMG-PCG's outer loop)
+    bool fusedOuter = false;
     bool trueResidualRestart = false;  // re-check ||b - Ax|| and restart if needed
     bool useGraph = true;
     bool useMega = true;     // PCG as one persistent cooperative launch when possible

@@ -47,7 +47,7 @@ __device__ __forceinline__ void reduce_and_finalize(double (&v)[K], const RSpec&
 // --------------------------------------------------------------------------
 // SELL-32 row helpers
 // --------------------------------------------------------------------------
-template <class T, int CK>
+template <class T, int CK, bool FM>
 __global__ void __launch_bounds__(kBlock) spmv_kernel(Rows<T> A, const T* __restrict__ x,
                                                       T* __restrict__ y, const T* dotWith,
                                                       RSpec red, Gate g)
@@ -55,23 +55,37 @@ __global__ void __launch_bounds__(kBlock) spmv_kernel(Rows<T> A, const T* __rest
     if (gate_closed(g)) return;
     double v[1] = {0.0};
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < A.n; r += gridDim.x * blockDim.x) {
-        T a = row_apply<T, XL_NC, true, CK>(A, r, x);
+        T a = row_apply<T, XL_NC, true, CK, FM>(A, r, x);
         y[r] = a;
-        if (dotWith) v[0] += (double)a * (double)dotWith[r];
+        if (dotWith) {
+            if constexpr (FM)
+                v[0] = fma((double)a, (double)dotWith[r], v[0]);
+            else
+                v[0] += (double)a * (double)dotWith[r];
+        }
     }
     if (red.blockPart) reduce_and_finalize<1>(v, red);
 }
 
 template <class T>
 void k_spmv(const Exec& ex, const Rows<T>& A, const T* x, T* y, const T* dotWith, RSpec red,
-            Gate g)
+            Gate g, bool fused)
 {
     if (A.n <= 0) return;
     const T* dw = red.blockPart ? dotWith : nullptr;
-    if (A.wide)
-        tick(), spmv_kernel<T, 16><<<ex.rowGrid(A.n, red), kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
-    else
-        tick(), spmv_kernel<T, 8><<<ex.rowGrid(A.n, red), kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
+    const dim3 grid = ex.rowGrid(A.n, red);
+    tick();
+    if (fused) {
+        if (A.wide)
+            spmv_kernel<T, 16, true><<<grid, kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
+        else
+            spmv_kernel<T, 8, true><<<grid, kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
+    } else {
+        if (A.wide)
+            spmv_kernel<T, 16, false><<<grid, kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
+        else
+            spmv_kernel<T, 8, false><<<grid, kBlock, 0, ex.s>>>(A, x, y, dw, red, g);
+    }
 }
 
 template <class T, int CK>
@@ -400,6 +414,17 @@ void diag_apply(const Exec& ex, int n, const double* rD, const double* r, double
 // --------------------------------------------------------------------------
 // PCG vector kernels (PCG.cpp:119-151)
 // --------------------------------------------------------------------------
+// FM: fused multiply-adds (see row_apply), for the mixed solve's outer loop
+template <bool FM>
+__device__ __forceinline__ double mad(double a, double b, double c)
+{
+    if constexpr (FM)
+        return fma(a, b, c);
+    else
+        return c + a * b;
+}
+
+template <bool FM>
 __global__ void __launch_bounds__(kBlock) pcg_direction_kernel(int n, const double* __restrict__ w,
                                                                double* __restrict__ p,
                                                                const KState* st, Gate g)
@@ -408,15 +433,21 @@ __global__ void __launch_bounds__(kBlock) pcg_direction_kernel(int n, const doub
     const bool useBeta = st->useBeta;
     const double beta = st->beta;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        p[i] = useBeta ? w[i] + beta * p[i] : w[i];
+        p[i] = useBeta ? mad<FM>(beta, p[i], w[i]) : w[i];
 }
 
-void k_pcg_direction(const Exec& ex, int n, const double* w, double* p, const KState* st, Gate g)
+void k_pcg_direction(const Exec& ex, int n, const double* w, double* p, const KState* st, Gate g,
+                     bool fused)
 {
     if (n <= 0) return;
-    tick(), pcg_direction_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, w, p, st, g);
+    tick();
+    if (fused)
+        pcg_direction_kernel<true><<<ex.grid(n), kBlock, 0, ex.s>>>(n, w, p, st, g);
+    else
+        pcg_direction_kernel<false><<<ex.grid(n), kBlock, 0, ex.s>>>(n, w, p, st, g);
 }
 
+template <bool FM>
 __global__ void __launch_bounds__(kBlock) pcg_update_kernel(int n, double* __restrict__ x,
                                                             double* __restrict__ r,
                                                             const double* __restrict__ p,
@@ -427,21 +458,26 @@ __global__ void __launch_bounds__(kBlock) pcg_update_kernel(int n, double* __res
     const double alpha = red.st->alpha;
     double v[1] = {0.0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        x[i] += alpha * p[i];
-        double ri = r[i] - alpha * q[i];
+        x[i] = mad<FM>(alpha, p[i], x[i]);
+        double ri = mad<FM>(-alpha, q[i], r[i]);
         r[i] = ri;
-        v[0] += ri * ri;
+        v[0] = mad<FM>(ri, ri, v[0]);
     }
     reduce_and_finalize<1>(v, red);
 }
 
 void k_pcg_update(const Exec& ex, int n, double* x, double* r, const double* p, const double* q,
-                  RSpec red, Gate g)
+                  RSpec red, Gate g, bool fused)
 {
     if (n <= 0) return;
-    tick(), pcg_update_kernel<<<ex.grid(n), kBlock, 0, ex.s>>>(n, x, r, p, q, red, g);
+    tick();
+    if (fused)
+        pcg_update_kernel<true><<<ex.grid(n), kBlock, 0, ex.s>>>(n, x, r, p, q, red, g);
+    else
+        pcg_update_kernel<false><<<ex.grid(n), kBlock, 0, ex.s>>>(n, x, r, p, q, red, g);
 }
 
+template <bool FM>
 __global__ void __launch_bounds__(kBlock) dot2_kernel(int n, const double* __restrict__ a,
                                                       const double* __restrict__ b,
                                                       const double* __restrict__ c,
@@ -451,16 +487,20 @@ __global__ void __launch_bounds__(kBlock) dot2_kernel(int n, const double* __res
     if (gate_closed(g)) return;
     double v[2] = {0.0, 0.0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        v[0] += a[i] * b[i];
-        if (c) v[1] += c[i] * d[i];
+        v[0] = mad<FM>(a[i], b[i], v[0]);
+        if (c) v[1] = mad<FM>(c[i], d[i], v[1]);
     }
     reduce_and_finalize<2>(v, red);
 }
 
 void k_dot2(const Exec& ex, int n, const double* a, const double* b, const double* c,
-            const double* d, RSpec red, Gate g)
+            const double* d, RSpec red, Gate g, bool fused)
 {
-    tick(), dot2_kernel<<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, a, b, c, d, red, g);
+    tick();
+    if (fused)
+        dot2_kernel<true><<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, a, b, c, d, red, g);
+    else
+        dot2_kernel<false><<<ex.grid(n > 0 ? n : 1), kBlock, 0, ex.s>>>(n, a, b, c, d, red, g);
 }
 
 // --------------------------------------------------------------------------
@@ -840,7 +880,8 @@ int device_max_blocks()
 // explicit instantiations
 // --------------------------------------------------------------------------
 #define INST(T)                                                                                   \
-    template void k_spmv<T>(const Exec&, const Rows<T>&, const T*, T*, const T*, RSpec, Gate);     \
+    template void k_spmv<T>(const Exec&, const Rows<T>&, const T*, T*, const T*, RSpec, Gate,      \
+                            bool);                                                               \
     template void k_residual<T>(const Exec&, const Rows<T>&, const T*, const T*, T*, RSpec, Gate); \
     template void k_gs_rows<T>(const Exec&, const Rows<T>&, T*, const T*, int, int, bool, Gate);   \
     template void gs_sweep<T>(const Exec&, const Level&, const Rows<T>&, T*, const T*, bool, bool, \

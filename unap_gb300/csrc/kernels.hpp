@@ -21,10 +21,12 @@ struct Rows {
 Rows<double> rows64(const Level& L);
 Rows<float> rows32(const Level& L);
 
-// y = A x; with a reduction spec, also sums y.dotWith (dotWith may be x)
+// y = A x; with a reduction spec, also sums y.dotWith (dotWith may be x).
+// fused: products and sums as fused multiply-adds (the mixed solve's outer
+// loop); otherwise the reference's separate roundings.
 template <class T>
 void k_spmv(const Exec& ex, const Rows<T>& A, const T* x, T* y, const T* dotWith, RSpec red,
-            Gate g);
+            Gate g, bool fused = false);
 
 // r = b - A x; with a reduction spec, sums r.r (sum0)
 template <class T>
@@ -54,14 +56,16 @@ void dic_apply(const Exec& ex, const Level& L, bool dilu, const double* rD, cons
 void diag_apply(const Exec& ex, int n, const double* rD, const double* r, double* w, RSpec red,
                 Gate g);
 
-// PCG pieces.  p = useBeta ? w + beta p : w
-void k_pcg_direction(const Exec& ex, int n, const double* w, double* p, const KState* st, Gate g);
+// PCG pieces (fused: fused multiply-adds, as for k_spmv).
+// p = useBeta ? w + beta p : w
+void k_pcg_direction(const Exec& ex, int n, const double* w, double* p, const KState* st, Gate g,
+                     bool fused = false);
 // x += alpha p, r -= alpha q; sums r.r
 void k_pcg_update(const Exec& ex, int n, double* x, double* r, const double* p, const double* q,
-                  RSpec red, Gate g);
+                  RSpec red, Gate g, bool fused = false);
 // sums a.b (and c.d when c != nullptr)
 void k_dot2(const Exec& ex, int n, const double* a, const double* b, const double* c,
-            const double* d, RSpec red, Gate g);
+            const double* d, RSpec red, Gate g, bool fused = false);
 
 // PBiCGStab pieces (PBiCGStab.cpp:155-456)
 void k_bicg_init(const Exec& ex, int n, const double* b, const double* Ax, double* r, double* r0,

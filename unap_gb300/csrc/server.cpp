@@ -184,6 +184,7 @@ void Server::largeWorker()
             K.relTol = r->relTol;
             K.maxIter = r->maxIter;
             K.flexible = flexible;
+            K.fusedOuter = r->method == SERVE_AMG_MIXED;
             K.trueResidualRestart = restart;
             // concurrent slots share the SMs: the persistent cooperative
             // executor needs every SM, so slots run per-step kernels,
