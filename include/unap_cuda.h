@@ -27,7 +27,10 @@
  * Part 2 adds unap_cuda_* entry points that have no counterpart in the
  * reference: device-pointer solves and kernels, AMG-PCG in FP64 and mixed
  * precision, batched and served solves.  They return 0 on success and a
- * negative code on error.
+ * negative code on error.  A call on device vectors runs after all work the
+ * caller issued before it to the legacy default stream (or any blocking
+ * stream), e.g. the fill of an initial guess, and returns when its results
+ * are in place.
  */
 #ifndef UNAP_CUDA_H
 #define UNAP_CUDA_H
@@ -400,6 +403,12 @@ int unap_cuda_batch_solve(long int batch, int count, const unap_cuda_batch_item*
 int unap_cuda_batch_destroy(long int batch);
 /* launch shape of the batch's last fused launch: CTA size, CTAs per system */
 int unap_cuda_batch_last_shape(long int batch, int* ctaThreads, int* clusterCtas);
+/* How the last batch solved its systems above the whole-solve size: 1 all
+ * in one group launch (thread-block clusters of 16 CTAs), 0 one after
+ * another with the per-step driver, -1 it had none.  The autotuner times
+ * both (iterations capped) for the first batch of each (size class, count
+ * class) and keeps the faster. */
+int unap_cuda_batch_large_mode(long int batch, int* mode);
 /* Systems of at most `cells` cells with an LDU preconditioner (none, Diag,
  * DIC, DILU) are solved by one whole-solve launch, in batches and by
  * unap_cuda_krylov_solve / pcgsolversolve_ / pbicgstabsolversolve_ alike

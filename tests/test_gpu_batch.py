@@ -160,3 +160,36 @@ def test_team_shape_autotuner(cuda):
     m.krylov_solve(0, 2, x, b, rel_tol=1e-9, max_iter=2000)
     assert capi.team_shape(s.n, 1) == (t, c)
     m.close()
+
+
+def test_large_systems_batch(cuda, orc):
+    """Systems above the whole-solve size: the autotuner picks one group
+    launch (clusters of 16 CTAs) or one solve after another; either way each
+    result matches the oracle, and the next batch of that class keeps the
+    choice."""
+    torch = cuda
+    cases = [(W.laplace(44, 42, 40, seed=71, permute=True, rhs="normal", shift=0.1), 0, 2),
+             (W.convdiff(42, 42, 40, seed=72, permute=True, pe=3.0), 1, 3),
+             (W.lognormal(46, 40, 40, seed=73, permute=True, sigma=1.0, shift=0.01), 0, 1)]
+    assert all(s.n > 65536 for s, _, _ in cases)
+    mats = [capi.DeviceMatrix(s) for s, _, _ in cases]
+    bs = [torch.tensor(s.b, device="cuda") for s, _, _ in cases]
+    B = capi.Batch()
+    modes = []
+    for rep in range(2):
+        xs = [torch.zeros(s.n, dtype=torch.float64, device="cuda") for s, _, _ in cases]
+        items = [dict(matrix=m, method=meth, precond=pc, x=x, b=b, rel_tol=1e-9, max_iter=3000)
+                 for m, (s, meth, pc), x, b in zip(mats, cases, xs, bs)]
+        stats, _ = B.solve(items)
+        modes.append(B.large_mode())
+        for (s, meth, pc), st, x in zip(cases, stats, xs):
+            fn = orc.pcg if meth == 0 else orc.pbicgstab
+            x_ref, st_ref = fn(s, pc, s.b, rel_tol=1e-9, max_iter=3000)
+            assert st["converged"], (s.name, st)
+            assert abs(st["nIterations"] - st_ref["n_iter"]) <= 1 or pc == 1, (s.name, st, st_ref)
+            d = orc.spmv(s, x.cpu().numpy() - x_ref)
+            assert np.linalg.norm(d) <= 2.2e-9 * st_ref["init_res"], s.name
+    assert modes[0] in (0, 1) and modes[1] == modes[0]
+    B.close()
+    for m in mats:
+        m.close()

@@ -149,6 +149,7 @@ SIGNATURES = {
     "unap_cuda_batch_solve": (_c_int, [_c_long, _c_int, _vp, _vp, _ip]),
     "unap_cuda_batch_destroy": (_c_int, [_c_long]),
     "unap_cuda_batch_last_shape": (_c_int, [_c_long, _ip, _ip]),
+    "unap_cuda_batch_large_mode": (_c_int, [_c_long, _ip]),
     "unap_cuda_set_team_solve_cells": (_c_int, [_c_int]),
     "unap_cuda_team_shape": (_c_int, [_c_int, _c_int, _ip, _ip]),
     "unap_cuda_force_team_shape": (_c_int, [_c_int, _c_int]),
@@ -202,6 +203,13 @@ class Batch:
         check(load().unap_cuda_batch_solve(self.handle, len(items), arr, stats,
                                            ctypes.byref(threads)))
         return [s.as_dict() for s in stats], threads.value
+
+    def large_mode(self):
+        """Systems above the whole-solve size in the last batch: 1 one group
+        launch, 0 one after another, -1 none."""
+        m = ctypes.c_int(0)
+        check(load().unap_cuda_batch_large_mode(self.handle, ctypes.byref(m)))
+        return m.value
 
     def last_shape(self):
         """(CTA size, CTAs per system) of the last fused launch."""

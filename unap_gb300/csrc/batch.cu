@@ -14,6 +14,7 @@
 // fastest is cached for the pair.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <map>
 #include <mutex>
 
@@ -79,17 +80,24 @@ void force_team_shape(int threads, int cluster)
     g_forceCluster = threads ? cluster : 0;
 }
 
-TeamShape cached_team_shape(int nMax, int m)
+// tuner cache key: large groups (clusters of 16 only) apart from the rest
+static std::pair<int, int> tune_key(int nMax, int m, bool largeGroup)
+{
+    return {size_class(nMax), count_class(m) + (largeGroup ? 1 : 0)};
+}
+
+TeamShape cached_team_shape(int nMax, int m, bool largeGroup)
 {
     if (g_forceThreads.load()) return TeamShape{g_forceThreads.load(), g_forceCluster.load()};
     std::lock_guard<std::mutex> lock(g_tune_mutex);
-    auto it = g_tuned.find({size_class(nMax), count_class(m)});
+    auto it = g_tuned.find(tune_key(nMax, m, largeGroup));
     return it == g_tuned.end() ? TeamShape{0, 0} : it->second;
 }
 
-TeamShape tuned_team_shape(cudaStream_t stream, const SmallSystem* dSys, int m, int nMax)
+TeamShape tuned_team_shape(cudaStream_t stream, const SmallSystem* dSys, int m, int nMax,
+                           bool largeGroup, float* bestMs)
 {
-    const TeamShape have = cached_team_shape(nMax, m);
+    const TeamShape have = cached_team_shape(nMax, m, largeGroup);
     if (have.threads) return have;
     std::vector<SmallSystem> sys((size_t)m);
     UNAP_CK(cudaMemcpyAsync(sys.data(), dSys, sizeof(SmallSystem) * (size_t)m,
@@ -130,7 +138,11 @@ TeamShape tuned_team_shape(cudaStream_t stream, const SmallSystem* dSys, int m, 
     float best = 1e30f;
     TeamShape bestS;
     for (int C : {1, 2, 4, 8, 16}) {
+        // systems above the whole-solve size: clusters of 16 CTAs of 256 or
+        // more threads only (smaller teams take many times longer there)
+        if (largeGroup && C != 16) continue;
         for (int t : {128, 256, 512, 1024}) {
+            if (largeGroup && t < 256) continue;
             if (C > 1 && small_team_capacity(t, C) <= 0) continue;
             copy_x(false);
             launch_small_krylov(stream, dWarm.p, m, nullptr, t, C);
@@ -153,9 +165,27 @@ TeamShape tuned_team_shape(cudaStream_t stream, const SmallSystem* dSys, int m, 
     cudaEventDestroy(e1);
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
-        g_tuned[{size_class(nMax), count_class(m)}] = bestS;
+        g_tuned[tune_key(nMax, m, largeGroup)] = bestS;
     }
+    if (bestMs) *bestMs = best;
     return bestS;
+}
+
+// large groups: whole-solve launch (1) or one system after another (0),
+// per (size class, count class); -1 while not measured
+static std::map<std::pair<int, int>, int> g_largeMode;
+
+int cached_large_mode(int nMax, int m)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_largeMode.find(tune_key(nMax, m, true));
+    return it == g_largeMode.end() ? -1 : it->second;
+}
+
+static void set_large_mode(int nMax, int m, int mode)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_largeMode[tune_key(nMax, m, true)] = mode;
 }
 
 BatchSolver::BatchSolver(cudaStream_t s) : stream(s) {}
@@ -205,21 +235,77 @@ std::vector<SolveStats> BatchSolver::solve(const std::vector<BatchItem>& items)
         (it.A->n() <= team_solve_cells() ? small : large).push_back((int)i);
     }
     if (!small.empty()) solveSmall(items, small, out);
-    for (int i : large) {
-        const BatchItem& it = items[(size_t)i];
-        auto P = make_ldu_precond(it.precond, *it.A);
-        Krylov K(*it.A, P.get(), it.method == 1 ? Method::PBiCGStab : Method::PCG);
-        K.tol = it.tol;
-        K.relTol = it.relTol;
-        K.maxIter = it.maxIter;
-        K.minIter = it.minIter;
-        out[(size_t)i] = K.solveDevice(it.x, it.b);
+    if (large.empty()) return out;
+    // Larger systems: one whole-solve launch for the group (clusters of 16
+    // CTAs, every system at once) or one system after another with the
+    // per-step driver (each over the whole GPU), whichever the autotuner
+    // measured faster for this (size class, count class): both run with
+    // iterations capped, the group's initial guesses restored after each.
+    int nMax = 0;
+    for (int i : large) nMax = std::max(nMax, items[(size_t)i].A->n());
+    const int m = (int)large.size();
+    int mode = m >= 2 ? cached_large_mode(nMax, m) : 0;
+    if (mode < 0) {
+        const double tSeq = timeSequential(items, large);
+        float tTeam = 1e30f;
+        solveSmall(items, large, out, true, &tTeam);
+        mode = tTeam < tSeq * 1e3 ? 1 : 0;
+        set_large_mode(nMax, m, mode);
+        lastLargeMode = mode;
+        return out;  // solved by the group launch already
     }
+    lastLargeMode = mode;
+    if (mode == 1) {
+        solveSmall(items, large, out, true, nullptr);
+        return out;
+    }
+    for (int i : large) out[(size_t)i] = solveOne(items[(size_t)i], items[(size_t)i].maxIter);
     return out;
 }
 
+SolveStats BatchSolver::solveOne(const BatchItem& it, int maxIter)
+{
+    auto P = make_ldu_precond(it.precond, *it.A);
+    Krylov K(*it.A, P.get(), it.method == 1 ? Method::PBiCGStab : Method::PCG);
+    K.tol = it.tol;
+    K.relTol = it.relTol;
+    K.maxIter = maxIter;
+    K.minIter = std::min(it.minIter, maxIter);
+    K.teamCells = 0;  // the per-step driver: this is the sequential arm
+    return K.solveDevice(it.x, it.b);
+}
+
+double BatchSolver::timeSequential(const std::vector<BatchItem>& items, const std::vector<int>& idx)
+{
+    // each system solved alone with its iterations capped; the caller's
+    // initial guesses are saved first and restored afterwards
+    size_t total = 0;
+    for (int i : idx) total += (size_t)items[(size_t)i].A->n();
+    DevArray<double> x0(total);
+    size_t off = 0;
+    for (int i : idx) {
+        const BatchItem& it = items[(size_t)i];
+        UNAP_CK(cudaMemcpyAsync(x0.p + off, it.x, sizeof(double) * (size_t)it.A->n(),
+                                cudaMemcpyDeviceToDevice, stream));
+        off += (size_t)it.A->n();
+    }
+    UNAP_CK(cudaStreamSynchronize(stream));
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int i : idx) (void)solveOne(items[(size_t)i], kTuneIters);
+    const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    off = 0;
+    for (int i : idx) {
+        const BatchItem& it = items[(size_t)i];
+        UNAP_CK(cudaMemcpyAsync(it.x, x0.p + off, sizeof(double) * (size_t)it.A->n(),
+                                cudaMemcpyDeviceToDevice, stream));
+        off += (size_t)it.A->n();
+    }
+    UNAP_CK(cudaStreamSynchronize(stream));
+    return t;
+}
+
 void BatchSolver::solveSmall(const std::vector<BatchItem>& items, const std::vector<int>& idx,
-                             std::vector<SolveStats>& out)
+                             std::vector<SolveStats>& out, bool largeGroup, float* tunedMs)
 {
     const int m = (int)idx.size();
     size_t total = 0;
@@ -274,7 +360,7 @@ void BatchSolver::solveSmall(const std::vector<BatchItem>& items, const std::vec
     if (!capturing()) count_launches(1);
     batch_perm_kernel<<<2 * m, 256, 0, stream>>>(reinterpret_cast<const PermJob*>(dIn.p));
 
-    const TeamShape shape = tuned_team_shape(stream, dSys.p, m, nMax);
+    const TeamShape shape = tuned_team_shape(stream, dSys.p, m, nMax, largeGroup, tunedMs);
     launch_small_krylov(stream, dSys.p, m, nullptr, shape.threads, shape.cluster);
     if (!capturing()) count_launches(1);
     batch_perm_kernel<<<m, 256, 0, stream>>>(reinterpret_cast<const PermJob*>(dOut.p));

@@ -31,6 +31,8 @@ public:
     ~BatchSolver();
     std::vector<SolveStats> solve(const std::vector<BatchItem>& items);
     TeamShape lastShape{0, 0};  // shape of the last fused launch
+    int lastLargeMode = -1;     // systems above the whole-solve size: 1 one
+                                // group launch, 0 one after another, -1 none
 
     // drop the cached preconditioner diagonals of a matrix that is going away
     void forget(const Matrix* A);
@@ -56,8 +58,14 @@ private:
     std::vector<DevArray<int>> waveDev;
     DevArray<unsigned char> dIn, dOut;  // gather / scatter job lists
     const double* factor(Matrix& A, int precond);
+    // the systems idx in one whole-solve launch (largeGroup: systems above
+    // the whole-solve size, clusters of 16 only); *tunedMs = the tuner's
+    // best capped time when it ran
     void solveSmall(const std::vector<BatchItem>& items, const std::vector<int>& idx,
-                    std::vector<SolveStats>& out);
+                    std::vector<SolveStats>& out, bool largeGroup = false,
+                    float* tunedMs = nullptr);
+    SolveStats solveOne(const BatchItem& it, int maxIter);
+    double timeSequential(const std::vector<BatchItem>& items, const std::vector<int>& idx);
 };
 
 // Shape of a fused launch of m systems (device array d_systems, largest
@@ -66,9 +74,13 @@ private:
 // launch of a pair times every launchable shape (CTA size 128 .. 1024 x
 // cluster 1 .. 16 CTAs) on these systems with the iterations capped, the
 // initial guesses restored after each trial, and caches the fastest.
-TeamShape tuned_team_shape(cudaStream_t s, const SmallSystem* d_systems, int m, int nMax);
+TeamShape tuned_team_shape(cudaStream_t s, const SmallSystem* d_systems, int m, int nMax,
+                           bool largeGroup = false, float* bestMs = nullptr);
 // the cached shape of a pair ({0, 0}: not tuned yet)
-TeamShape cached_team_shape(int nMax, int m);
+TeamShape cached_team_shape(int nMax, int m, bool largeGroup = false);
+// systems above the whole-solve size in a batch: 1 one group launch, 0 one
+// after another, -1 not measured yet for this pair
+int cached_large_mode(int nMax, int m);
 // every later launch uses this shape instead of the tuner's (threads 0:
 // back to the tuner)
 void force_team_shape(int threads, int cluster);

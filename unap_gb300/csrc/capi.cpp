@@ -551,6 +551,7 @@ int unap_cuda_spmv(long int handle, const double* x, double* y)
     return guarded([&] {
         MatHandle* h = mat_from(handle);
         Matrix& A = h->get();
+        order_after_default_stream(A.stream);
         Exec ex{A.stream, device_max_blocks()};
         h->ensureScratch();
         k_to_internal<double>(ex, A.n(), A.L->d_perm.p, x, h->s1.p);
@@ -566,6 +567,7 @@ int unap_cuda_precondition(long int handle, int precond, const double* r, double
     return guarded([&] {
         MatHandle* h = mat_from(handle);
         Matrix& A = h->get();
+        order_after_default_stream(A.stream);
         Exec ex{A.stream, device_max_blocks()};
         h->ensureScratch();
         auto P = make_ldu_precond(precond, A);
@@ -582,6 +584,7 @@ int unap_cuda_gauss_seidel(long int handle, double* x, const double* b, int nSwe
     return guarded([&] {
         MatHandle* h = mat_from(handle);
         Matrix& A = h->get();
+        order_after_default_stream(A.stream);
         if (!A.L->sweepable)
             throw std::invalid_argument(
                 "Gauss-Seidel needs oriented, owner-sorted faces and a matrix built with "
@@ -607,6 +610,7 @@ int unap_cuda_krylov_solve(long int handle, int method, int precond, double tol,
         Matrix& A = mat_from(handle)->get();
         auto P = make_ldu_precond(precond, A);
         Krylov K(A, P.get(), method == 1 ? Method::PBiCGStab : Method::PCG);
+        order_after_default_stream(A.stream);
         K.tol = tol;
         K.relTol = relTol;
         K.maxIter = maxIter;

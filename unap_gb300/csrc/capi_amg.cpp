@@ -161,6 +161,7 @@ int unap_cuda_amg_vcycle(long int amg, const double* r, double* z)
     return guarded([&] {
         AmgHandle* h = amg_from(amg);
         Matrix& A = *h->A;
+        order_after_default_stream(A.stream);
         Exec ex{A.stream, device_max_blocks()};
         const int n = A.n();
         DevArray<double> ri((size_t)n), zi((size_t)n);
@@ -218,6 +219,7 @@ int unap_cuda_amg_solve(long int amg, double* x, const double* b, unap_cuda_stat
 {
     return guarded([&] {
         AmgHandle* h = amg_from(amg);
+        order_after_default_stream(h->A->stream);
         put(h->K->solveDevice(x, b), stats);
     });
 }

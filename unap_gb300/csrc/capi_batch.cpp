@@ -85,6 +85,8 @@ int unap_cuda_batch_solve(long int batch, int count, const unap_cuda_batch_item*
         }
         // the matrices' own streams finish their setup before the batch runs
         for (const BatchItem& b : v) UNAP_CK(cudaStreamSynchronize(b.A->stream));
+        // and the caller's vectors, filled on the default stream, are ready
+        order_after_default_stream(h->stream);
         std::vector<SolveStats> st = h->S->solve(v);
         for (int i = 0; i < count && stats; ++i) {
             stats[i].nIterations = st[(size_t)i].nIter;
@@ -107,6 +109,14 @@ int unap_cuda_batch_last_shape(long int batch, int* ctaThreads, int* clusterCtas
         BatchHandle* h = batch_from(batch);
         if (ctaThreads) *ctaThreads = h->S->lastShape.threads;
         if (clusterCtas) *clusterCtas = h->S->lastShape.cluster;
+    });
+}
+
+int unap_cuda_batch_large_mode(long int batch, int* mode)
+{
+    return guarded([&] {
+        BatchHandle* h = batch_from(batch);
+        if (mode) *mode = h->S->lastLargeMode;
     });
 }
 

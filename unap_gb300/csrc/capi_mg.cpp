@@ -226,7 +226,11 @@ int unap_cuda_mg_levels(long int mg, int* nCoarseLevels, int* cells, int maxOut)
 
 int unap_cuda_mg_solve(long int mg, double* x, const double* b, unap_cuda_stats* stats)
 {
-    return guarded([&] { mg_solve_device(mg_from(mg), x, b, stats); });
+    return guarded([&] {
+        MgHandle* h = mg_from(mg);
+        order_after_default_stream(h->A->stream);
+        mg_solve_device(h, x, b, stats);
+    });
 }
 
 int unap_cuda_mg_solve_host(long int mg, double* x, const double* b, unap_cuda_stats* stats)

@@ -175,7 +175,9 @@ __global__ void __launch_bounds__(kBlock, (CK == 8 && sizeof(T) == 4) ? 6 : 1)
                                                            T c2, int first, Gate g)
 {
     // the next step's kernel may launch now; before the wait this kernel
-    // reads only the matrix and b, which no kernel of the step chain writes
+    // reads only the matrix, which no kernel writes (b may have just been
+    // written by the previous kernel, a restriction: it is read after the
+    // wait, with x and w)
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     int len = 0, base = 0;
@@ -186,7 +188,6 @@ __global__ void __launch_bounds__(kBlock, (CK == 8 && sizeof(T) == 4) ? 6 : 1)
         len = lds<true>(A.rowInfo + r) & 0xffff;
         base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
         d = lds<true>(A.diag + r);
-        bb = ldg(b + r);
 #pragma unroll
         for (int k = 0; k < CK; ++k) {
             const int e = base + 32 * k;
@@ -196,6 +197,7 @@ __global__ void __launch_bounds__(kBlock, (CK == 8 && sizeof(T) == 4) ? 6 : 1)
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
     if (gate_closed(g) || r >= A.n) return;
+    bb = __ldcg(b + r);
     // A x in the reference's order: 0, + diag x, then the row's faces
     const T xr = xin[r];
     T xv[CK];

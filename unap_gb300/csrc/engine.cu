@@ -78,6 +78,17 @@ void pinned_block_free(void* p)
     if (it == g_pinnedSize.end()) return;
     g_pinnedFree[it->second].push_back(p);
 }
+void order_after_default_stream(cudaStream_t s)
+{
+    // an event on the legacy default stream, waited for by s: everything
+    // issued before the call to the legacy stream (and so to every blocking
+    // stream) is done before s runs the call's kernels
+    cudaEvent_t e;
+    UNAP_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    UNAP_CK(cudaEventRecord(e, cudaStreamLegacy));
+    UNAP_CK(cudaStreamWaitEvent(s, e, 0));
+    UNAP_CK(cudaEventDestroy(e));  // released once it has completed
+}
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 const char* last_error() { return g_last_error.c_str(); }
 

@@ -125,9 +125,10 @@ __global__ void __launch_bounds__(kBlock) gs_kernel(Rows<T> A, T* x, const T* __
                                                     int r0, int r1, int skipUpper, Gate g)
 {
     // Programmatic dependent launch: the next wavefront's kernel may begin
-    // launching now.  Before griddepcontrol.wait a kernel reads only data no
-    // kernel of the sweep writes (matrix streams and b); x and the solver
-    // state are read after it, when the previous kernel has completed.
+    // launching now.  Before griddepcontrol.wait a kernel reads only the
+    // matrix, which no kernel writes; b (the previous kernel may have just
+    // written it: a restriction, a conversion), x and the solver state are
+    // read after it, when the previous kernel's writes are visible.
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     int r = r0 + blockIdx.x * blockDim.x + threadIdx.x;
     int info = 0, base = 0;
@@ -138,7 +139,6 @@ __global__ void __launch_bounds__(kBlock) gs_kernel(Rows<T> A, T* x, const T* __
         info = lds<true>(A.rowInfo + r);
         base = ldg(A.sliceOff + (r >> 5)) + (r & 31);
         d = lds<true>(A.diag + r);
-        bb = lds<true>(b + r);
         const int len = info & 0xffff;
 #pragma unroll
         for (int k = 0; k < CK; ++k) {
@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(kBlock) gs_kernel(Rows<T> A, T* x, const T* __
     asm volatile("griddepcontrol.wait;" ::: "memory");
     if (gate_closed(g)) return;
     if (r < r1) {
+        bb = __ldcg(b + r);
         const int jEnd = skipUpper ? (info >> 16) : (info & 0xffff);
         T xv[CK];
 #pragma unroll
@@ -174,8 +175,15 @@ __global__ void __launch_bounds__(kBlock) gs_kernel(Rows<T> A, T* x, const T* __
 }
 
 static std::atomic<int> g_pdl{1};
+static thread_local int g_pdlThread = -1;  // this thread's override (-1: none)
 int set_wave_pdl(int on) { return g_pdl.exchange(on ? 1 : 0); }
-bool wave_pdl() { return g_pdl.load() != 0; }
+int set_thread_wave_pdl(int mode)
+{
+    const int old = g_pdlThread;
+    g_pdlThread = mode;
+    return old;
+}
+bool wave_pdl() { return g_pdlThread >= 0 ? g_pdlThread != 0 : g_pdl.load() != 0; }
 static std::atomic<int> g_rowGrid{1};
 int set_wave_grid(int oneRowPerThread) { return g_rowGrid.exchange(oneRowPerThread ? 1 : 0); }
 
@@ -198,7 +206,7 @@ static void launch_gs(const Exec& ex, const Rows<T>& A, T* x, const T* b, int r0
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = g_pdl.load() ? 1 : 0;
+    cfg.numAttrs = wave_pdl() ? 1 : 0;
     tick();
     UNAP_CK(cudaLaunchKernelEx(&cfg, gs_kernel<T, CK>, A, x, b, r0, r1, skipUpper, g));
 }

@@ -116,6 +116,9 @@ void k_axpby(const Exec& ex, int n, T a, const T* x, T b, T* y, Gate g);  // y =
 // next wavefront's kernel launches while the previous one runs and loads its
 // matrix data before waiting); 0 turns it off.  Returns the previous value.
 int set_wave_pdl(int on);
+// this host thread's setting, over the process-wide one: 0 off, 1 on, -1
+// follow the process-wide one; returns the previous override
+int set_thread_wave_pdl(int mode);
 bool wave_pdl();
 // Wavefront Gauss-Seidel grids: 1 (default) one row per thread, 0 a
 // grid-stride loop over at most SMs x 8 CTAs.  Returns the previous value.

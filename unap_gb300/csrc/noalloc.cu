@@ -102,6 +102,7 @@ extern "C" int unap_cuda_spmv_noalloc(long int handle, const double* x, double* 
         double* xi = scratch;
         double* yi = scratch + kNoAllocMaxCells;
         Exec ex{A.stream, device_max_blocks()};
+        order_after_default_stream(A.stream);
         k_to_internal<double>(ex, n, A.L->d_perm.p, x, xi);
         k_spmv<double>(ex, rows64(*A.L), xi, yi, nullptr, RSpec{}, Gate{});
         k_to_reference<double>(ex, n, A.L->d_perm.p, yi, y);

@@ -132,6 +132,11 @@ void Server::largeWorker()
     // in this stream's order: a slot's setup never synchronizes the device
     // (and so never waits for the other slots' solves)
     StreamAllocScope scope(s);
+    // Programmatic dependent launch off in the slots: a dependent kernel's
+    // CTAs launched early wait on SMs the other slots' kernels could use
+    // (8 concurrent PCG+DIC solves of 373k cells: 36.7 solves/s without it,
+    // 22.1 with it)
+    set_thread_wave_pdl(0);
     for (;;) {
         ServeRequest* r = nullptr;
         {
@@ -218,6 +223,7 @@ void Server::batchWorker()
     cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     {
         StreamAllocScope scope(s);
+        set_thread_wave_pdl(0);
         BatchSolver B(s);
         for (;;) {
             std::vector<ServeRequest*> take;

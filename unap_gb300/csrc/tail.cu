@@ -677,7 +677,8 @@ __global__ void __launch_bounds__(kBlock) gs_packed_kernel(const int2* __restric
     constexpr int EPR = Pk<T>::EPR;
     constexpr int R = KW / EPR;
     // the next wavefront's kernel may launch now; before the wait this
-    // kernel reads only data no kernel of the sweep writes
+    // kernel reads only the matrix, which no kernel writes (b may have just
+    // been written by the previous kernel: it is read after the wait)
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int r = r0 + blockIdx.x * blockDim.x + threadIdx.x;
     int start = 0, info = 0;
@@ -688,7 +689,6 @@ __global__ void __launch_bounds__(kBlock) gs_packed_kernel(const int2* __restric
         start = m.x;
         info = m.y;
         d = ldg(diag + r);
-        bb = ldg(b + r);
         const int len = info & 0xffff;
 #pragma unroll
         for (int k = 0; k < R; ++k)
@@ -696,6 +696,7 @@ __global__ void __launch_bounds__(kBlock) gs_packed_kernel(const int2* __restric
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
     if (gate_closed(g) || r >= r1) return;
+    bb = __ldcg(b + r);
     const int jEnd = skipUpper ? (info >> 16) : (info & 0xffff);
     T xv[KW];
 #pragma unroll

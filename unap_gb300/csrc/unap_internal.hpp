@@ -115,6 +115,13 @@ struct StreamAllocScope {
     StreamAllocScope& operator=(const StreamAllocScope&) = delete;
 };
 
+// Calls on caller-owned device vectors run on the matrix's own
+// (non-blocking) stream; this orders that stream after all work the caller
+// issued before the call to the legacy default stream or any blocking
+// stream (e.g. the fill of an initial guess), so the call reads its inputs
+// as the caller left them.
+void order_after_default_stream(cudaStream_t s);
+
 // Small pinned host blocks (solver state read back every iteration) from a
 // process-wide free list: cudaFreeHost would synchronize the device.
 void* pinned_block_alloc(size_t bytes);
