@@ -1224,8 +1224,10 @@ int orc_dense_spd_inverse(int n, const double* A, double* inv)
  *   level k < L:  x = 0; nPre forward GS sweeps; r = b - A x (reference SpMV
  *                 order); b' = restrict(r); e = V(k+1, b'); x += prolong(e);
  *                 nPost backward GS sweeps.
- *   level L:      x = Ainv b, Ainv the dense inverse above, each row summed
- *                 in ascending column order from 0.
+ *   level L:      x = Ainv b, Ainv the dense inverse above; each row is
+ *                 summed in chunks of ORC_DENSE_CHUNK columns, each chunk in
+ *                 ascending order from 0, the chunk sums added in order from
+ *                 0 (orc_dense_row).
  * precision 1 runs every level matrix, vector and sweep in FP32 (values
  * rounded from FP64), with the coarsest product in FP64.
  *
@@ -1475,6 +1477,23 @@ static void amg_cheby32(oamg* g, int k, float* x, const float* b, int fromZero)
     free(p);
 }
 
+/* Row i of the coarsest product: the columns in chunks of ORC_DENSE_CHUNK,
+ * each chunk summed in ascending order from 0, then the chunk sums added in
+ * chunk order from 0.  (A chunked sum keeps the dependency chain short on
+ * the GPU, where chunks are summed by separate threads.) */
+#define ORC_DENSE_CHUNK 64
+static double orc_dense_row(const double* Ainv, int n, int i, const double* b)
+{
+    double t = 0.0;
+    for (int j0 = 0; j0 < n; j0 += ORC_DENSE_CHUNK) {
+        const int j1 = j0 + ORC_DENSE_CHUNK < n ? j0 + ORC_DENSE_CHUNK : n;
+        double p = 0.0;
+        for (int j = j0; j < j1; ++j) p += Ainv[(size_t)i * (size_t)n + (size_t)j] * b[j];
+        t += p;
+    }
+    return t;
+}
+
 static void amg_vcycle64(oamg* g, int k)
 {
     int L = g->nLv - 1;
@@ -1482,11 +1501,7 @@ static void amg_vcycle64(oamg* g, int k)
     const double* b = g->b[k];
     if (k == L) {
         int n = g->nc;
-        for (int i = 0; i < n; ++i) {
-            double t = 0.0;
-            for (int j = 0; j < n; ++j) t += g->Ainv[(size_t)i * (size_t)n + (size_t)j] * b[j];
-            x[i] = t;
-        }
+        for (int i = 0; i < n; ++i) x[i] = orc_dense_row(g->Ainv, n, i, b);
         return;
     }
     omat* A = (omat*)g->A[k];
@@ -1517,12 +1532,10 @@ static void amg_vcycle32(oamg* g, int k)
     const float* b = g->bf[k];
     if (k == L) {
         int n = g->nc;
-        for (int i = 0; i < n; ++i) {
-            double t = 0.0;
-            for (int j = 0; j < n; ++j)
-                t += g->Ainv[(size_t)i * (size_t)n + (size_t)j] * (double)b[j];
-            x[i] = (float)t;
-        }
+        double* bd = (double*)xcalloc((size_t)n, sizeof(double));
+        for (int j = 0; j < n; ++j) bd[j] = (double)b[j];
+        for (int i = 0; i < n; ++i) x[i] = (float)orc_dense_row(g->Ainv, n, i, bd);
+        free(bd);
         return;
     }
     const fmat* A = &g->F[k];

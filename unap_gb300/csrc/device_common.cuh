@@ -207,6 +207,26 @@ __device__ __forceinline__ T row_subtract(const Rows<T>& A, const T* coef, int b
     return acc;
 }
 
+// Row i of the AMG coarsest product x = Minv b (Minv column-major, b staged
+// in sb as FP64): the columns in chunks of kDenseChunk, each chunk summed
+// in ascending order from 0, the chunk sums added in chunk order from 0.
+// dense_apply_kernel sums the chunks in separate threads; this one-thread
+// form gives the same bits.
+constexpr int kDenseChunk = 64;
+__device__ __forceinline__ double dense_row_chunked(const double* M, int n, int i,
+                                                    const double* sb)
+{
+    double t = 0.0;
+    for (int j0 = 0; j0 < n; j0 += kDenseChunk) {
+        const int j1 = min(j0 + kDenseChunk, n);
+        double p = 0.0;
+#pragma unroll 16
+        for (int j = j0; j < j1; ++j) p += __ldg(M + (size_t)j * n + i) * sb[j];
+        t += p;
+    }
+    return t;
+}
+
 // --- finalize operations (run by one thread) -----------------------------
 
 // do { ... } while (++nIter < maxIter && !checkConvergence(...)),

@@ -691,23 +691,41 @@ void k_prolong_add(const Exec& ex, int nFine, const int* cmap, const T* coarse, 
         tick(), prolong_add_kernel<T><<<ex.grid(nFine), kBlock, 0, ex.s>>>(nFine, cmap, coarse, fine, g);
 }
 
-// Dense coarsest solve: x_i = sum_j Minv[i][j] b_j, j ascending, FP64.
-// b is staged in shared memory as FP64; thread i walks column-major Minv so
-// a warp reads 32 consecutive rows of one column per step.
-// gather (optional) maps column j to its entry of b, so the sum runs in the
-// column order of M even when b is in another order.
+// Coarsest level of the AMG V-cycle: x = Minv b with the dense FP64 inverse
+// (column-major; column j holds Minv[.][j] with rows in the level's internal
+// order), accumulated in FP64.  Each row is summed in chunks of kDenseChunk
+// columns (dense_row_chunked's order): a CTA takes 32 consecutive rows, and
+// warp q of it the chunks q, q + nWarps, ... of those rows (a warp reads 32
+// consecutive rows of one column per step); the chunk sums meet in shared
+// memory and the first warp adds them in chunk order.  The dependency chain
+// of a row is 64 + n / 64 additions instead of n.  gather (optional) maps
+// column j to its entry of b.
 template <class T>
 __global__ void dense_apply_kernel(int n, const double* __restrict__ M, const T* __restrict__ b,
                                    const int* __restrict__ gather, T* __restrict__ x, Gate g)
 {
     if (gate_closed(g)) return;
-    extern __shared__ double sb[];
+    extern __shared__ double sm[];
+    double* sb = sm;  // b, n entries
+    const int nChunks = (n + kDenseChunk - 1) / kDenseChunk;
+    double* part = sm + n;  // [chunk][32 rows]
     for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = (double)b[gather ? gather[j] : j];
     __syncthreads();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double t = 0.0;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int i = blockIdx.x * 32 + lane;
+    for (int q = w; q < nChunks; q += nw) {
+        double p = 0.0;
+        if (i < n) {
+            const int j0 = q * kDenseChunk, j1 = min(j0 + kDenseChunk, n);
 #pragma unroll 16
-        for (int j = 0; j < n; ++j) t += ldg(M + (size_t)j * n + i) * sb[j];
+            for (int j = j0; j < j1; ++j) p += ldg(M + (size_t)j * n + i) * sb[j];
+        }
+        part[q * 32 + lane] = p;
+    }
+    __syncthreads();
+    if (w == 0 && i < n) {
+        double t = 0.0;
+        for (int q = 0; q < nChunks; ++q) t += part[q * 32 + lane];
         x[i] = (T)t;
     }
 }
@@ -717,10 +735,14 @@ void k_dense_apply(const Exec& ex, int n, const double* MinvColMajor, const T* b
                    T* x, Gate g)
 {
     if (n <= 0) return;
-    int threads = 64;
-    int blocks = div_up(n, threads);
-    tick(), dense_apply_kernel<T><<<blocks, threads, (size_t)n * sizeof(double), ex.s>>>(
-        n, MinvColMajor, b, gather, x, g);
+    const int nChunks = (n + kDenseChunk - 1) / kDenseChunk;
+    const int threads = 32 * std::min(nChunks, 32);
+    const size_t smem = (size_t)(n + 32 * nChunks) * sizeof(double);
+    if (smem > 48 * 1024)  // coarsest levels above 4,096 cells (the limit is 8,192)
+        UNAP_CK(cudaFuncSetAttribute(dense_apply_kernel<T>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    tick(), dense_apply_kernel<T><<<div_up(n, 32), threads, smem, ex.s>>>(n, MinvColMajor, b,
+                                                                          gather, x, g);
 }
 
 template <class T>

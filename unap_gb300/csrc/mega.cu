@@ -147,12 +147,7 @@ __device__ void exec_dense(const Step& s, int first, int stride, bool single)
     const double* M = (const double*)s.e;
     for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = (double)b[s.i0 ? s.i0[j] : j];
     __syncthreads();
-    for (int i = first; i < n; i += stride) {
-        double t = 0.0;
-#pragma unroll 16
-        for (int j = 0; j < n; ++j) t += ldg(M + (size_t)j * n + i) * sb[j];
-        x[i] = (T)t;
-    }
+    for (int i = first; i < n; i += stride) x[i] = (T)dense_row_chunked(M, n, i, sb);
     (void)single;
 }
 

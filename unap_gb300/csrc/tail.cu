@@ -362,8 +362,9 @@ __device__ void restrict_stage(const TailLevel& F, T* bNext, const Ctx& c)
     cluster_barrier();
 }
 
-// x_c = Minv b_c in FP64, j ascending (dense_apply_kernel); x_c is
-// cluster-distributed, each warp computes one 32-row slice
+// x_c = Minv b_c in FP64, in dense_row_chunked's order (as
+// dense_apply_kernel); x_c is cluster-distributed, each warp computes one
+// 32-row slice
 template <class T>
 __device__ __noinline__ void coarsest_stage(const TailArgs& a, double* sb, Ctx c)
 {
@@ -373,12 +374,7 @@ __device__ __noinline__ void coarsest_stage(const TailArgs& a, double* sb, Ctx c
     __syncthreads();
     const unsigned xOffB = (unsigned)(a.xcOff * (int)sizeof(T));
     for_units<true>(c, a.nc, [&](int i) {
-        double t = 0.0;
-        // unrolled so many independent column loads are in flight; the sum
-        // itself stays in j order
-#pragma unroll 16
-        for (int j = 0; j < a.nc; ++j) t += ldg(a.Minv + (size_t)j * a.nc + i) * sb[j];
-        xmine<T, true>(c, dyn, xOffB, i) = (T)t;
+        xmine<T, true>(c, dyn, xOffB, i) = (T)dense_row_chunked(a.Minv, a.nc, i, sb);
     });
     cluster_barrier();
 }
