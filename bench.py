@@ -78,6 +78,12 @@ L2_BYTES = 129 * 2 ** 20
 # one ncu capture of a smaller case; the roofline's `traffic` scales it to
 # the launch group's algorithmic bytes (the traffic grows with the rows)
 TRAFFIC_RATIO = {
+    "gs_kernel<float>": (
+        471.9 / 366.7,
+        "ncu dram__bytes_read.sum + dram__bytes_write.sum of the 19 wavefront launches of one "
+        "FP32 forward sweep of the 192^3 finest level, caches as the program left them: "
+        "471.9 MB against 366.7 MB algorithmic, scaled by the launch group's algorithmic "
+        "bytes"),
     "cheb_step_kernel<float>": (
         327.9 / 258.9,
         "ncu dram__bytes_read.sum + dram__bytes_write.sum of one Chebyshev step on level 1 "
@@ -732,12 +738,12 @@ def setup_case(args):
     print(json.dumps(out), flush=True)
 
 
-def smoother_roofline(G, info, mixed: bool, peak: float, deg: int):
+def smoother_roofline(G, info, mixed: bool, peak: float, deg: int, sweeps: int):
     """Per-level smoother launch groups of the V-cycle timed with CUDA events
     (unap_cuda_amg_profile_smoother), and the kernel family with the largest
     device time per V-cycle: Chebyshev steps (2 deg - 1 launches per level
     and V-cycle: the first pre-smoothing step runs inside the restriction)
-    or Gauss-Seidel sweeps (nPre + nPost = 4 per level)."""
+    or Gauss-Seidel sweeps (`sweeps` = nPre + nPost per level)."""
     fam = {"cheb": {"ms": 0.0, "bytes": 0.0, "levels": []},
            "gs_fine": {"ms": 0.0, "bytes": 0.0, "levels": []},
            "gs_coarse": {"ms": 0.0, "bytes": 0.0, "levels": []}}
@@ -746,7 +752,7 @@ def smoother_roofline(G, info, mixed: bool, peak: float, deg: int):
     for k in range(info["n_levels"] - 1):
         ms, by, launches = G.profile_smoother(k, reps=10)
         cheb = lam[k] > 0
-        reps = (2 * deg - 1) if cheb else 4
+        reps = (2 * deg - 1) if cheb else sweeps
         f = "cheb" if cheb else ("gs_fine" if k == 0 else "gs_coarse")
         fam[f]["ms"] += reps * ms
         fam[f]["bytes"] += reps * by
@@ -894,7 +900,8 @@ def main():
     peak_src = ("measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                 else "fallback 6.8 TB/s")
     deg = kw.get("cheby_degree", 3)
-    top, groups, per_level = smoother_roofline(G, info, mixed, peak, deg)
+    top, groups, per_level = smoother_roofline(G, info, mixed, peak, deg,
+                                               kw.get("n_pre", 2) + kw.get("n_post", 2))
     vprof = G.profile_vcycle(reps=10)
     mprof = A.profile(reps=10)
     spmv = {"kernel": "spmv_kernel<double>", "ms": mprof["spmv"],

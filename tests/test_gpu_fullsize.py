@@ -134,3 +134,29 @@ def test_c4_full(cuda, orc):
     assert d <= 1e-6, d
     assert abs(sols[1][0] - sols[0][0]) <= 5, (sols[1][0], sols[0][0])
     A.close()
+
+
+def test_c4_headline_vcycle(cuda, orc):
+    """The benchmark's V-cycle (Gauss-Seidel 1/1 on levels 0-1, Chebyshev
+    degree 3 on [lambda/60, 1.1 lambda] below) at full 256^3: the mixed and
+    FP64 solves both reach a 1e-10 true relative residual (b - A x by the
+    oracle's SpMV) and agree within 1e-8."""
+    torch = cuda
+    s = W.config("c4")
+    b = dev(torch, s.b)
+    A = capi.DeviceMatrix(s)
+    kw = dict(smoother=1, cheby_degree=3, cheby_from=2, eig_ratio=60.0, n_pre=1, n_post=1)
+    sols = {}
+    for prec in (1, 0):
+        G = capi.DeviceAmg(A, n_coarsest=1000, precision=prec, rel_tol=1e-10, **kw)
+        x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+        st = G.solve(x, b)
+        assert st["converged"], (prec, st)
+        xh = x.cpu().numpy()
+        assert true_rel(orc, s, xh) <= 1.0001e-10, prec
+        sols[prec] = (st["nIterations"], xh)
+        G.close()
+    d = np.linalg.norm(sols[1][1] - sols[0][1]) / np.linalg.norm(sols[0][1])
+    assert d <= 1e-8, d
+    assert abs(sols[1][0] - sols[0][0]) <= 3, (sols[1][0], sols[0][0])
+    A.close()
