@@ -460,6 +460,10 @@ int unap_cuda_set_server_graphs(int on);
  * thread-block cluster (default: every size; 0: per-step launches);
  * returns the previous value */
 int unap_cuda_set_server_team_cells(int cells);
+/* AMG requests of the server: coarsest level target (default 200 cells)
+ * and the Chebyshev interval [lambda / eigRatio, 1.1 lambda] (default 30),
+ * for requests started afterwards */
+int unap_cuda_set_server_amg(int nCoarsest, double eigRatio);
 
 int unap_cuda_device_synchronize(void);
 

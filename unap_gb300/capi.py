@@ -155,6 +155,7 @@ SIGNATURES = {
     "unap_cuda_force_team_shape": (_c_int, [_c_int, _c_int]),
     "unap_cuda_set_server_graphs": (_c_int, [_c_int]),
     "unap_cuda_set_server_team_cells": (_c_int, [_c_int]),
+    "unap_cuda_set_server_amg": (_c_int, [_c_int, _c_dbl]),
     "unap_cuda_server_create": (_c_int, [_lp, _c_ll, _c_int, _c_int]),
     "unap_cuda_server_submit": (_c_int, [_c_long, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp,
                                          _c_int, _c_dbl, _c_int, ctypes.POINTER(_c_ll)]),
@@ -344,6 +345,11 @@ def set_server_graphs(on: bool) -> bool:
     """Server slots replay Krylov iterations from CUDA graphs (default) or
     launch kernel by kernel; returns the previous setting."""
     return bool(load().unap_cuda_set_server_graphs(1 if on else 0))
+
+
+def set_server_amg(n_coarsest: int = 200, eig_ratio: float = 30.0) -> None:
+    """Server AMG requests: coarsest level target and Chebyshev ratio."""
+    check(load().unap_cuda_set_server_amg(int(n_coarsest), float(eig_ratio)))
 
 
 def set_server_team_cells(cells: int) -> int:

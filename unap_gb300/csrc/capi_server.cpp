@@ -113,4 +113,9 @@ int unap_cuda_set_server_graphs(int on) { return set_server_graphs(on); }
 
 int unap_cuda_set_server_team_cells(int cells) { return set_server_team_cells(cells); }
 
+int unap_cuda_set_server_amg(int nCoarsest, double eigRatio)
+{
+    return guarded([&] { set_server_amg(nCoarsest, eigRatio); });
+}
+
 }  // extern "C"

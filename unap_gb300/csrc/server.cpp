@@ -10,7 +10,21 @@ namespace unapgpu {
 namespace {
 std::atomic<int> g_serverGraphs{1};
 std::atomic<int> g_serverTeamCells{0};
+// AMG requests: coarsest level target.  200 rather than the headline's
+// 1000: the coarsest dense inverse (one launch per column) is a large part
+// of a small request's setup (400 requests of the serving stream: 39.6
+// solves/s against 37.7 with 1000)
+std::atomic<int> g_serverCoarsest{200};
+std::atomic<int> g_serverEigRatio10{300};  // AMG requests: Chebyshev ratio x 10
 }  // namespace
+
+void set_server_amg(int nCoarsest, double eigRatio)
+{
+    if (nCoarsest < 2 || !(eigRatio > 1.0))
+        throw std::invalid_argument("server AMG: nCoarsest >= 2 and eigRatio > 1");
+    g_serverCoarsest = nCoarsest;
+    g_serverEigRatio10 = (int)(eigRatio * 10.0 + 0.5);
+}
 
 int server_graphs() { return g_serverGraphs.load(); }
 int set_server_graphs(int on) { return g_serverGraphs.exchange(on ? 1 : 0); }
@@ -174,7 +188,8 @@ void Server::largeWorker()
                 ap.smoother = 1;
                 ap.chebyDegree = 3;
                 ap.chebyFrom = 0;
-                ap.eigRatio = 30.0;
+                ap.eigRatio = g_serverEigRatio10.load() / 10.0;
+                ap.nCoarsest = g_serverCoarsest.load();
                 H = std::make_unique<AmgHierarchy>(A, ap);
                 P = std::make_unique<AmgPrecond>(*H);
                 flexible = ap.precision == 1;

@@ -46,6 +46,9 @@ int set_server_graphs(int on);
 // batch lane) solves run as one whole-solve launch (default: all; 0: never);
 // returns the previous value.
 int set_server_team_cells(int cells);
+// AMG requests: coarsest level target (default 200 cells) and Chebyshev
+// interval ratio (default 30), for requests started afterwards
+void set_server_amg(int nCoarsest, double eigRatio);
 
 struct ServerParams {
     long long memoryBudget = 0;  // bytes; 0: 80% of free device memory at start
