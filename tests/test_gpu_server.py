@@ -16,12 +16,21 @@ pytestmark = pytest.mark.gpu
 
 
 def alone(torch, s, method, rel_tol):
-    A = capi.DeviceMatrix(s)
+    """The same solve outside the server, with the server's method: AMG
+    requests on a matrix without wavefronts, Chebyshev degree 3 on every
+    level ([lambda/30, 1.1 lambda]), coarsest level of 200 cells."""
+    amg = method in ("amg_mixed", "amg_fp64")
+    old = capi.set_matrix_wavefronts(not amg)
+    try:
+        A = capi.DeviceMatrix(s)
+    finally:
+        capi.set_matrix_wavefronts(old)
     x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
     b = torch.tensor(s.b, device="cuda")
-    if method in ("amg_mixed", "amg_fp64"):
+    if amg:
         G = capi.DeviceAmg(A, precision=1 if method == "amg_mixed" else 0, rel_tol=rel_tol,
-                           max_iter=1000)
+                           max_iter=1000, n_coarsest=200, smoother=1, cheby_degree=3,
+                           cheby_from=0, eig_ratio=30.0)
         st = G.solve(x, b)
         G.close()
     else:
