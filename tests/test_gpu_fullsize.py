@@ -86,6 +86,19 @@ def test_c2_full(cuda, orc):
     assert np.linalg.norm(xg - x_ref) <= 1e-10 * np.linalg.norm(x_ref)
     O.close()
     G.close()
+    # the mixed-precision solve (FP32 V-cycle, FP64 outer PCG, the
+    # benchmark's smoothers) against the FP64 oracle's solution: at relTol
+    # 1e-10 its error is the convergence tolerance's, not the FP32 V-cycle's
+    G = capi.DeviceAmg(A, n_coarsest=1000, precision=1, rel_tol=1e-10, smoother=1,
+                       cheby_degree=3, cheby_from=2, eig_ratio=60.0, n_pre=1, n_post=1)
+    x.zero_()
+    st = G.solve(x, dev(torch, s.b))
+    assert st["converged"]
+    xm = x.cpu().numpy()
+    assert true_rel(orc, s, xm) <= 1.0001e-10
+    err = np.linalg.norm(xm - x_ref) / np.linalg.norm(x_ref)
+    assert err <= 1e-8, err
+    G.close()
     A.close()
 
 
