@@ -67,6 +67,7 @@ def test_c2_full(cuda, orc):
     st = G.solve(x, dev(torch, s.b))
     assert st["converged"]
     xg = x.cpu().numpy()
+    x64 = xg.copy()  # the FP64 GPU solve at relTol 1e-10
     assert true_rel(orc, s, xg) <= 1.0001e-10
     # the oracle's own FP64 AMG-PCG at full size: the same iteration count
     # +-1 and agreement in residual space at relTol 1e-10, and solutions
@@ -87,8 +88,9 @@ def test_c2_full(cuda, orc):
     O.close()
     G.close()
     # the mixed-precision solve (FP32 V-cycle, FP64 outer PCG, the
-    # benchmark's smoothers) against the FP64 oracle's solution: at relTol
-    # 1e-10 its error is the convergence tolerance's, not the FP32 V-cycle's
+    # benchmark's smoothers) against the FP64 oracle's solution (relTol
+    # 1e-13): at relTol 1e-10 its error is the convergence tolerance's, as
+    # large as the FP64 solve's at the same tolerance and not more
     G = capi.DeviceAmg(A, n_coarsest=1000, precision=1, rel_tol=1e-10, smoother=1,
                        cheby_degree=3, cheby_from=2, eig_ratio=60.0, n_pre=1, n_post=1)
     x.zero_()
@@ -96,8 +98,11 @@ def test_c2_full(cuda, orc):
     assert st["converged"]
     xm = x.cpu().numpy()
     assert true_rel(orc, s, xm) <= 1.0001e-10
-    err = np.linalg.norm(xm - x_ref) / np.linalg.norm(x_ref)
-    assert err <= 1e-8, err
+    nref = np.linalg.norm(x_ref)
+    err_mixed = np.linalg.norm(xm - x_ref) / nref
+    err_fp64 = np.linalg.norm(x64 - x_ref) / nref
+    print(f"c2 error against the FP64 oracle: mixed {err_mixed:.3e}, FP64 {err_fp64:.3e}")
+    assert err_mixed <= 10 * err_fp64 + 1e-12, (err_mixed, err_fp64)
     G.close()
     A.close()
 
