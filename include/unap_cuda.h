@@ -537,6 +537,12 @@ int unap_cuda_set_matrix_wavefronts(int on);
  * previous setting, or UNAP_CUDA_EINVAL for another value.  No counterpart
  * in the reference. */
 int unap_cuda_set_cheby_chunk(int entries);
+/* Chebyshev V-cycles run their coarse levels of at most `rows` rows (and
+ * every level below them, at most 8 above the coarsest) in one
+ * thread-block-cluster launch instead of a launch per step (0: never).
+ * Results are identical.  Returns the previous value; applies to AMG
+ * handles created afterwards.  No counterpart in the reference. */
+int unap_cuda_set_cheby_tail_rows(int rows);
 
 /* Coarse-level tail of the AMG V-cycle (per-step executor), set for the FP64
  * (precision 0) or FP32 (precision 1) V-cycle: every level with at most

@@ -83,6 +83,47 @@ def test_cheby_eigenvalues_and_vcycle_bit_exact(cuda, orc, precision, case):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("case", [0, 1, 4])
+def test_cheby_cluster_tail_bit_exact(cuda, orc, precision, case):
+    """The coarse Chebyshev levels in one cluster launch (from the first
+    Chebyshev level below 1,000 rows, or from level 1): the same V-cycle
+    bits as the oracle's, and the same solve as with a launch per step."""
+    torch = cuda
+    for rows in (1000, 1 << 30):
+        old = capi.set_cheby_tail_rows(rows)
+        try:
+            for s in spd_systems():
+                A, G, O = _pair(orc, s, precision, CASES[case])
+                O.set_eigs(G.eigenvalues())
+                r = np.random.default_rng(s.n).standard_normal(s.n)
+                z = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+                G.vcycle(dev(torch, r), z)
+                assert np.array_equal(z.cpu().numpy(), O.vcycle(r)), (s.name, precision, rows)
+                G.close()
+                O.close()
+                A.close()
+        finally:
+            capi.set_cheby_tail_rows(old)
+    s = W.lognormal(30, 28, 26, seed=19, permute=True)
+    A = capi.DeviceMatrix(s)
+    b = dev(torch, s.b)
+    res = []
+    for rows in (0, 5000):
+        old = capi.set_cheby_tail_rows(rows)
+        try:
+            G = capi.DeviceAmg(A, n_coarsest=100, precision=precision, smoother=1,
+                               rel_tol=1e-9, **CASES[case])
+        finally:
+            capi.set_cheby_tail_rows(old)
+        x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+        st = G.solve(x, b)
+        res.append((st["nIterations"], x.cpu().numpy()))
+        G.close()
+    assert res[0][0] == res[1][0] and np.array_equal(res[0][1], res[1][1])
+    A.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
 def test_cheby_launch_geometry_same_bits(cuda, precision):
     """One-warp or 256-thread CTAs and 8- or 16-entry load chunks for the
     Chebyshev steps: same bits."""

@@ -154,6 +154,7 @@ SIGNATURES = {
     "unap_cuda_team_shape": (_c_int, [_c_int, _c_int, _ip, _ip]),
     "unap_cuda_force_team_shape": (_c_int, [_c_int, _c_int]),
     "unap_cuda_set_server_graphs": (_c_int, [_c_int]),
+    "unap_cuda_set_cheby_tail_rows": (_c_int, [_c_int]),
     "unap_cuda_set_server_team_cells": (_c_int, [_c_int]),
     "unap_cuda_set_server_amg": (_c_int, [_c_int, _c_dbl]),
     "unap_cuda_server_create": (_c_int, [_lp, _c_ll, _c_int, _c_int]),
@@ -339,6 +340,13 @@ def set_team_solve_cells(cells: int) -> int:
     """Systems of at most `cells` cells with an LDU preconditioner are solved
     by one whole-solve launch (0: never); returns the previous value."""
     return int(load().unap_cuda_set_team_solve_cells(int(cells)))
+
+
+def set_cheby_tail_rows(rows: int) -> int:
+    """Chebyshev V-cycles run their levels of at most `rows` rows (and all
+    below) in one cluster launch (0: never), for AMG handles created
+    afterwards; returns the previous value."""
+    return int(load().unap_cuda_set_cheby_tail_rows(int(rows)))
 
 
 def set_server_graphs(on: bool) -> bool:

@@ -181,6 +181,17 @@ AmgHierarchy::AmgHierarchy(Matrix& A_, const AmgParams& p) : params(p), A(A_)
     phase(4);
     if (params.smoother == 1) setupCheby(s);
     tail_cluster_size();  // function attributes and the cluster query, outside any capture
+    // the Chebyshev levels of at most cheby_tail_rows() rows, and all below,
+    // in one cluster launch
+    if (params.smoother == 1 && cheby_tail_rows() > 0 && cheby_tail_cluster() > 0) {
+        for (int k = std::max(1, params.chebyFrom); k < L; ++k)
+            if (lv[(size_t)k].n <= cheby_tail_rows() && L - k <= kChebTailMaxLevels) {
+                chebTail = k;
+                break;
+            }
+        if (chebTail > 0)
+            chebTailPart.alloc((size_t)nc * (size_t)((nc + kDenseChunk - 1) / kDenseChunk));
+    }
     phase(5);
     setupSeconds =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -404,6 +415,44 @@ void AmgHierarchy::sweep(const Exec& ex, int k, const Level& Lk, const Rows<T>& 
 }
 
 template <class T>
+ChebTailArgs<T> AmgHierarchy::chebTailArgs(int k)
+{
+    const int L = nLevels() - 1;
+    ChebTailArgs<T> a{};
+    a.nLev = L - k;
+    a.deg = params.chebyDegree;
+    for (int l = 0; l < a.nLev; ++l) {
+        const int kk = k + l;
+        Lv& V = lv[(size_t)kk];
+        ChebTailLevel<T>& t = a.lev[l];
+        t.A = rowsT<T>(*V.L);
+        t.childStart = V.childStart.p;
+        t.child = V.child.p;
+        t.cmap = V.cmap.p;
+        t.x = X<T>(kk);
+        t.b = B<T>(kk);
+        t.w = R<T>(kk);
+        t.cb[0] = chebBuf<T>(kk, 0);
+        t.cb[1] = chebBuf<T>(kk, 1);
+        t.post = (params.chebyDegree % 2 == 0) ? X<T>(kk) : Tmp<T>(kk);
+        t.Rth = (T)V.Rth;
+        for (int j = 0; j < kChebyMaxDegree; ++j) {
+            t.d1[j] = (T)V.d1[j];
+            t.d2[j] = (T)V.d2[j];
+        }
+    }
+    a.nc = nc;
+    a.cChildStart = lv[(size_t)L].childStart.p;
+    a.cChild = lv[(size_t)L].child.p;
+    a.cCmap = lv[(size_t)L].cmap.p;
+    a.cb = B<T>(L);
+    a.cx = X<T>(L);
+    a.Minv = Minv.p;
+    a.part = chebTailPart.p;
+    return a;
+}
+
+template <class T>
 void AmgHierarchy::vcycle_level(const Exec& ex, int k, Gate g)
 {
     const int L = nLevels() - 1;
@@ -412,6 +461,11 @@ void AmgHierarchy::vcycle_level(const Exec& ex, int k, Gate g)
     if (profIn) UNAP_CK(cudaEventRecordWithFlags((*profIn)[(size_t)k], ex.s, cudaEventRecordExternal));
     if (k == curTail && k < L) {
         launch_tail<T>(ex, k, g);
+        if (profOut) UNAP_CK(cudaEventRecordWithFlags((*profOut)[(size_t)k], ex.s, cudaEventRecordExternal));
+        return;
+    }
+    if (k == chebTail) {
+        launch_cheb_tail<T>(ex, chebTailArgs<T>(k), g);
         if (profOut) UNAP_CK(cudaEventRecordWithFlags((*profOut)[(size_t)k], ex.s, cudaEventRecordExternal));
         return;
     }

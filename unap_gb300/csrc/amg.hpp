@@ -134,6 +134,11 @@ private:
     void sweep(const Exec& ex, int k, const Level& Lk, const Rows<T>& Rk, T* x, const T* b,
                bool backward, bool xIsZero, Gate g);
     int curTail = -1;
+    // first level of the Chebyshev cluster tail (launch_cheb_tail), -1: none
+    int chebTail = -1;
+    DevArray<double> chebTailPart;  // its coarsest chunk sums
+    template <class T>
+    ChebTailArgs<T> chebTailArgs(int k);
     std::vector<cudaEvent_t>* profIn = nullptr;   // per-level events (profiling)
     std::vector<cudaEvent_t>* profOut = nullptr;
     template <class T>

@@ -270,6 +270,8 @@ int unap_cuda_set_packed_sweeps(int mode) { return set_packed_sweeps(mode); }
 
 int unap_cuda_set_cheby_small_rows(int rows) { return set_cheby_small_rows(rows); }
 
+int unap_cuda_set_cheby_tail_rows(int rows) { return set_cheby_tail_rows(rows); }
+
 int unap_cuda_set_matrix_wavefronts(int on) { return set_matrix_wavefronts(on); }
 
 int unap_cuda_set_cheby_chunk(int entries)

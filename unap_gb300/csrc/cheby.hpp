@@ -74,6 +74,59 @@ template <class T>
 void k_prolong_add_to(const Exec& ex, int n, const int* cmap, const T* coarse, const T* xin,
                       T* xout, Gate g);
 
+// ---- the coarse end of a Chebyshev V-cycle in one cluster launch --------
+constexpr int kChebTailMaxLevels = 8;
+
+// one tail level: its matrix, the restriction into it (children of each
+// cell, ascending), the prolongation out of it (cmap: finer row -> cell),
+// its vectors (x, b, w = the residual buffer, the two buffers of the step
+// chain: step j writes cb[j & 1], the post-smoothing chain starting from
+// `post`) and Chebyshev coefficients
+template <class T>
+struct ChebTailLevel {
+    Rows<T> A;
+    const int* childStart;
+    const int* child;
+    const int* cmap;
+    T* x;
+    T* b;
+    T* w;
+    T* cb[2];
+    T* post;
+    T Rth;
+    T d1[kChebyMaxDegree];
+    T d2[kChebyMaxDegree];
+};
+
+template <class T>
+struct ChebTailArgs {
+    ChebTailLevel<T> lev[kChebTailMaxLevels];  // first tail level .. coarsest - 1
+    int nLev;
+    int deg;
+    int nc;                   // coarsest level
+    const int* cChildStart;   // restriction into it
+    const int* cChild;
+    const int* cCmap;         // prolongation out of it
+    T* cb;
+    T* cx;
+    const double* Minv;       // dense inverse, column-major
+    double* part;             // nc x ceil(nc / 64) chunk sums (scratch)
+};
+
+// One launch of a thread-block cluster (16 CTAs of 512 threads, else 8)
+// runs the V-cycle from a.lev[0] (its b, first iterate and w already set by
+// the fused restriction) down to the coarsest and back, bit-identical to the
+// per-step kernels.
+template <class T>
+void launch_cheb_tail(const Exec& ex, const ChebTailArgs<T>& a, Gate g);
+// Chebyshev V-cycles run their levels of at most `rows` rows (and every
+// level below them) in the tail launch; 0 turns it off.  Returns the
+// previous value; applies to hierarchies built afterwards.
+int set_cheby_tail_rows(int rows);
+int cheby_tail_rows();
+// cluster size the tail launches with on this device (0: none schedulable)
+int cheby_tail_cluster();
+
 // Rows per level below which Chebyshev-step launches use one-warp CTAs
 // (spread over more SMs); returns the previous value.
 int set_cheby_small_rows(int rows);

@@ -211,8 +211,7 @@ __device__ __forceinline__ T row_subtract(const Rows<T>& A, const T* coef, int b
 // in sb as FP64): the columns in chunks of kDenseChunk, each chunk summed
 // in ascending order from 0, the chunk sums added in chunk order from 0.
 // dense_apply_kernel sums the chunks in separate threads; this one-thread
-// form gives the same bits.
-constexpr int kDenseChunk = 64;
+// form gives the same bits.  (kDenseChunk: kernels.hpp)
 __device__ __forceinline__ double dense_row_chunked(const double* M, int n, int i,
                                                     const double* sb)
 {

@@ -21,6 +21,10 @@ struct Rows {
 Rows<double> rows64(const Level& L);
 Rows<float> rows32(const Level& L);
 
+// columns per chunk of the AMG coarsest product's row sums (each chunk
+// summed in order, then the chunk sums in order)
+constexpr int kDenseChunk = 64;
+
 // y = A x; with a reduction spec, also sums y.dotWith (dotWith may be x).
 // fused: products and sums as fused multiply-adds (the mixed solve's outer
 // loop); otherwise the reference's separate roundings.
