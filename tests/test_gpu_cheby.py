@@ -99,6 +99,8 @@ def test_cheby_cluster_tail_bit_exact(cuda, orc, precision, case):
                 z = torch.zeros(s.n, dtype=torch.float64, device="cuda")
                 G.vcycle(dev(torch, r), z)
                 assert np.array_equal(z.cpu().numpy(), O.vcycle(r)), (s.name, precision, rows)
+                prof = G.profile_vcycle(reps=2)  # the tail's first level holds its time
+                assert prof["vcycle_ms"] > 0 and min(prof["level_ms"]) >= 0
                 G.close()
                 O.close()
                 A.close()

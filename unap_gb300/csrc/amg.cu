@@ -795,8 +795,11 @@ int AmgHierarchy::profile(cudaStream_t s, int reps, double* ms, int maxOut)
         UNAP_CK(cudaEventCreate(&in[(size_t)k]));
         UNAP_CK(cudaEventCreate(&out[(size_t)k]));
     }
-    // levels below a tail record no events: start them at the tail's time
-    const int tail = tailFirst(params.precision == 1 ? sizeof(float) : sizeof(double));
+    // levels below a tail (the Gauss-Seidel cluster tail or the Chebyshev
+    // one) record no events: the tail's first level holds the whole tail
+    const int tail = chebTail >= 0
+                         ? chebTail
+                         : tailFirst(params.precision == 1 ? sizeof(float) : sizeof(double));
     // one V-cycle captured as a CUDA graph (as inside a solve), with an
     // event node around every level
     cudaGraph_t gr = nullptr;
