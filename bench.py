@@ -591,6 +591,36 @@ def serve_bench(n_requests: int, seed: int = 0, max_slots: int = 12, compare_pla
     return out
 
 
+def krylov_case(args):
+    """One solve of a Krylov config (c1 or c3) through the reference's method,
+    timed with CUDA events after `--warmup` solves (the small case for the
+    whole-solve launch's profile); `--team-shape T,C` forces the launch
+    shape of the whole-solve launch (c1's size)."""
+    import torch
+    from unap_gb300 import capi
+    from unap_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    name = args.krylov_config
+    cfg = CONFIGS[name]
+    if cfg["kind"] != "krylov":
+        raise SystemExit(f"{name} is not a Krylov config")
+    if args.team_shape:
+        t, c = (int(v) for v in args.team_shape.split(","))
+        capi.force_team_shape(t, c)
+    s = W.config(name, args.scale, seed=0)
+    A = capi.DeviceMatrix(s)
+    b = torch.tensor(s.b, device="cuda")
+    x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    for _ in range(args.warmup + 1):
+        x.zero_()
+        st = A.krylov_solve(cfg["method"], cfg["precond"], x, b, rel_tol=cfg["rel_tol"],
+                            max_iter=5000)
+    print(json.dumps({"config": name, "cells": s.n, "iterations": st["nIterations"],
+                      "seconds": st["seconds"], "shape": capi.team_shape(s.n, 1)}), flush=True)
+    A.close()
+
+
 def kernels_case(args):
     """Finest-level kernels of the workload's matrix, each launched on its own
     and timed with CUDA events (SpMV, DIC/DILU, Gauss-Seidel sweeps FP64 and
@@ -797,6 +827,10 @@ def main():
                     help="only time the finest-level kernels one launch at a time "
                          "(the small case for kernel profiles) and exit")
     ap.add_argument("--reps", type=int, default=5, help="repetitions for --kernels")
+    ap.add_argument("--krylov-config", default="", choices=["", "c1", "c3"],
+                    help="only run one solve of this Krylov config (after --warmup) and exit")
+    ap.add_argument("--team-shape", default="",
+                    help="with --krylov-config: force the whole-solve launch shape 'T,C'")
     ap.add_argument("--profile-solve", action="store_true",
                     help="bracket one extra mixed solve after the timed ones (with --setup: "
                          "the device setup) with cudaProfilerStart/Stop, for ncu "
@@ -819,6 +853,9 @@ def main():
         raise SystemExit("--warmup must be >= 3")
     if args.kernels:
         kernels_case(args)
+        return
+    if args.krylov_config:
+        krylov_case(args)
         return
     if args.smoother_level >= 0:
         smoother_case(args)
