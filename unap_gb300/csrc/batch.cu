@@ -47,6 +47,7 @@ __global__ void batch_perm_kernel(const PermJob* jobs)
 
 std::mutex g_tune_mutex;
 std::map<std::pair<int, int>, TeamShape> g_tuned;  // (size class, count class) -> shape
+std::map<std::pair<int, int>, float> g_tunedMs;    // the shape's capped trial time
 std::atomic<int> g_teamCells{kTeamSolveCells};
 std::atomic<int> g_forceThreads{0}, g_forceCluster{0};  // shape override (0: tuner)
 constexpr int kTuneIters = 10;  // iterations per timed trial
@@ -98,7 +99,15 @@ TeamShape tuned_team_shape(cudaStream_t stream, const SmallSystem* dSys, int m, 
                            bool largeGroup, float* bestMs)
 {
     const TeamShape have = cached_team_shape(nMax, m, largeGroup);
-    if (have.threads) return have;
+    if (have.threads) {
+        // a forced shape was never timed: *bestMs is left as it is
+        if (bestMs && !g_forceThreads.load()) {
+            std::lock_guard<std::mutex> lock(g_tune_mutex);
+            auto it = g_tunedMs.find(tune_key(nMax, m, largeGroup));
+            if (it != g_tunedMs.end()) *bestMs = it->second;
+        }
+        return have;
+    }
     std::vector<SmallSystem> sys((size_t)m);
     UNAP_CK(cudaMemcpyAsync(sys.data(), dSys, sizeof(SmallSystem) * (size_t)m,
                             cudaMemcpyDeviceToHost, stream));
@@ -166,6 +175,7 @@ TeamShape tuned_team_shape(cudaStream_t stream, const SmallSystem* dSys, int m, 
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         g_tuned[tune_key(nMax, m, largeGroup)] = bestS;
+        g_tunedMs[tune_key(nMax, m, largeGroup)] = best;
     }
     if (bestMs) *bestMs = best;
     return bestS;
@@ -247,10 +257,14 @@ std::vector<SolveStats> BatchSolver::solve(const std::vector<BatchItem>& items)
     int mode = m >= 2 ? cached_large_mode(nMax, m) : 0;
     if (mode < 0) {
         const double tSeq = timeSequential(items, large);
-        float tTeam = 1e30f;
+        float tTeam = -1.0f;
         solveSmall(items, large, out, true, &tTeam);
-        mode = tTeam < tSeq * 1e3 ? 1 : 0;
-        set_large_mode(nMax, m, mode);
+        if (tTeam >= 0.0f) {
+            mode = tTeam < tSeq * 1e3 ? 1 : 0;
+            set_large_mode(nMax, m, mode);
+        } else {
+            mode = 1;  // a forced shape, never timed: nothing is cached
+        }
         lastLargeMode = mode;
         return out;  // solved by the group launch already
     }

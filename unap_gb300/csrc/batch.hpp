@@ -59,8 +59,9 @@ private:
     DevArray<unsigned char> dIn, dOut;  // gather / scatter job lists
     const double* factor(Matrix& A, int precond);
     // the systems idx in one whole-solve launch (largeGroup: systems above
-    // the whole-solve size, clusters of 16 only); *tunedMs = the tuner's
-    // best capped time when it ran
+    // the whole-solve size, clusters of 16 only); *tunedMs = the chosen
+    // shape's capped trial time (timed now or cached with the shape), left
+    // as it is for a forced shape
     void solveSmall(const std::vector<BatchItem>& items, const std::vector<int>& idx,
                     std::vector<SolveStats>& out, bool largeGroup = false,
                     float* tunedMs = nullptr);

@@ -117,10 +117,15 @@ long long Server::submit(std::unique_ptr<ServeRequest> r)
 std::unique_ptr<ServeRequest> Server::wait(long long id)
 {
     std::unique_lock<std::mutex> lk(mu);
+    if (all.find(id) == all.end()) throw std::invalid_argument("unknown request id");
+    // looked up again after every wake-up: another thread waiting on the
+    // same id may have collected the request meanwhile
+    doneCv.wait(lk, [&] {
+        auto j = all.find(id);
+        return j == all.end() || j->second->done;
+    });
     auto it = all.find(id);
-    if (it == all.end()) throw std::invalid_argument("unknown request id");
-    ServeRequest* r = it->second.get();
-    doneCv.wait(lk, [&] { return r->done; });
+    if (it == all.end()) throw std::invalid_argument("request already collected");
     std::unique_ptr<ServeRequest> out = std::move(it->second);
     all.erase(it);
     return out;
@@ -130,10 +135,13 @@ void Server::finish(ServeRequest* r)
 {
     r->tEnd = now_seconds();
     {
+        // the budget is released under the lock: a worker between its
+        // admission check (false) and its wait holds the lock, so the
+        // release and the notification below cannot fall in that window
         std::lock_guard<std::mutex> lk(mu);
         r->done = true;
+        used -= r->bytes;
     }
-    used -= r->bytes;
     doneCv.notify_all();
     cv.notify_all();
 }
