@@ -433,7 +433,8 @@ int unap_cuda_force_team_shape(int ctaThreads, int clusterCtas);
  * on their own streams so their work overlaps on the GPU; PCG/PBiCGStab
  * requests of at most smallCells cells are collected and solved together
  * in one fused launch.  wait() blocks until the request is done, copies x
- * (host) and reports timings measured from submission. */
+ * (host) and reports timings measured from submission; a request is
+ * collected once (a second wait on its id returns UNAP_CUDA_EINVAL). */
 typedef struct {
     int status;     /* 0 ok */
     int batched;    /* solved in a fused small-system launch */
@@ -457,8 +458,9 @@ int unap_cuda_server_destroy(long int server);
 int unap_cuda_set_server_graphs(int on);
 /* PCG/PBiCGStab requests of up to `cells` cells that a server slot solves
  * (those above the batch lane's size) run as one whole-solve launch on a
- * thread-block cluster (default: every size; 0: per-step launches);
- * returns the previous value */
+ * thread-block cluster (default 0: none, every slot request runs per-step
+ * launches, which serve the mixed stream faster); returns the previous
+ * value */
 int unap_cuda_set_server_team_cells(int cells);
 /* AMG requests of the server: coarsest level target (default 200 cells)
  * and the Chebyshev interval [lambda / eigRatio, 1.1 lambda] (default 30),
