@@ -272,8 +272,11 @@ int unap_cuda_agglomeration_destroy(long int aggl);
 int unap_cuda_gauss_seidel(long int handle, double* x, const double* b, int nSweeps,
                            int backward);
 
-/* PCG (method 0) or PBiCGStab (method 1) with an LDU preconditioner on
- * device vectors; x holds the initial guess on entry. */
+/* PCG (method 0) or PBiCGStab (method 1) with an LDU preconditioner
+ * (precond 0 none, 1 Diag, 2 DIC, 3 DILU; other codes return
+ * UNAP_CUDA_EINVAL, unlike the Fortran-convention calls, which fall back to
+ * none as the reference does) on device vectors; x holds the initial guess
+ * on entry. */
 int unap_cuda_krylov_solve(long int handle, int method, int precond, double tol, double relTol,
                            int maxIter, int minIter, double* x, const double* b,
                            unap_cuda_stats* stats);

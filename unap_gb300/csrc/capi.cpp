@@ -608,6 +608,10 @@ int unap_cuda_krylov_solve(long int handle, int method, int precond, double tol,
 {
     return guarded([&] {
         Matrix& A = mat_from(handle)->get();
+        if (method != 0 && method != 1)
+            throw std::invalid_argument("method 0 (PCG) or 1 (PBiCGStab)");
+        if (precond < 0 || precond > 3)
+            throw std::invalid_argument("precond 0 (none), 1 (Diag), 2 (DIC) or 3 (DILU)");
         auto P = make_ldu_precond(precond, A);
         Krylov K(A, P.get(), method == 1 ? Method::PBiCGStab : Method::PCG);
         order_after_default_stream(A.stream);

@@ -69,9 +69,16 @@ int unap_cuda_batch_solve(long int batch, int count, const unap_cuda_batch_item*
 {
     return guarded([&] {
         BatchHandle* h = batch_from(batch);
+        if (count < 0 || (count > 0 && !items))
+            throw std::invalid_argument("batch: count >= 0 and an item array");
         std::vector<BatchItem> v((size_t)count);
         for (int i = 0; i < count; ++i) {
             const unap_cuda_batch_item& it = items[i];
+            if (it.method != 0 && it.method != 1)
+                throw std::invalid_argument("batch item: method 0 (PCG) or 1 (PBiCGStab)");
+            if (it.precond < 0 || it.precond > 3)
+                throw std::invalid_argument("batch item: precond 0 (none), 1 (Diag), 2 (DIC) or 3 "
+                                            "(DILU)");
             BatchItem& b = v[(size_t)i];
             b.A = &mat_from(it.matrix)->get();
             b.method = it.method;
