@@ -252,6 +252,7 @@ class Server:
         check(load().unap_cuda_server_create(ctypes.byref(h), memory_budget, max_slots,
                                              small_cells))
         self.handle = h.value
+        self._cells = {}  # request id -> nCells (the size of x that wait() fills)
 
     def submit(self, system, method, rel_tol=1e-8, max_iter=1000):
         l = _i32(system.lower_addr)
@@ -267,10 +268,17 @@ class Server:
                                              None if lo is None else lo.ctypes.data,
                                              d.ctypes.data, up.ctypes.data, b.ctypes.data, m,
                                              rel_tol, max_iter, ctypes.byref(rid)))
+        self._cells[rid.value] = int(system.n)
         return rid.value
 
-    def wait(self, rid, n):
-        x = np.zeros(n)
+    def wait(self, rid, n=None):
+        cells = self._cells.pop(rid, None)
+        if n is not None and cells is not None and n != cells:
+            self._cells[rid] = cells
+            raise ValueError(f"request {rid} has {cells} cells, not {n}")
+        if cells is None and n is None:
+            raise ValueError(f"unknown request {rid}: pass its number of cells")
+        x = np.zeros(cells if cells is not None else n)
         info = RequestInfo()
         check(load().unap_cuda_server_wait(self.handle, rid, x.ctypes.data, ctypes.byref(info)))
         return x, info.as_dict()
