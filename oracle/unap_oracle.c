@@ -382,9 +382,25 @@ static void diag_pcg_loops(const omat* m, double* x, const double* b, const doub
 }
 
 /* computeMaxEig + computeValueForMatrix + determineEigRange + h14Sturm,
- * eigenDiagPCG.cpp:242-361 (tridiagonal Lanczos matrix, Sturm bisection) */
+ * eigenDiagPCG.cpp:242-361 (tridiagonal Lanczos matrix, Sturm bisection).
+ *
+ * One departure, on input the reference never finishes: when the diagonal
+ * PCG stops early (wArA below VSMALL, e.g. a system of two or three cells
+ * solved exactly), the reference still builds the tridiagonal matrix from
+ * all nDiagPCGs iterations, the missing alphas are 0, the matrix holds
+ * infinities and its bisection never ends.  Here, as in the CUDA path, the
+ * matrix stops at the first iteration that did not run (one row: 1 /
+ * alpha_0; none: 1) and the bisection at 4096 halvings.  Whenever the
+ * diagonal PCG runs all its iterations the result is the reference's, bit
+ * for bit. */
 static double compute_max_eig(const double* alphas, const double* betas, int nP)
 {
+    {
+        int ran = 0;
+        while (ran < nP && alphas[ran] != 0.0) ++ran;
+        nP = ran;
+    }
+    if (nP < 2) return nP == 1 ? 1.0 / alphas[0] : 1.0;
     double* T = (double*)xcalloc((size_t)nP * (size_t)nP, sizeof(double));
 #define T_(i, j) T[(size_t)(i) * (size_t)nP + (size_t)(j)]
     for (int i = 0; i < nP; ++i) {
@@ -406,6 +422,7 @@ static double compute_max_eig(const double* alphas, const double* betas, int nP)
     }
     double* p = (double*)xcalloc((size_t)nP, sizeof(double));
     double xn;
+    int halvings = 0;
     do {
         xn = (xBegin + xEnd) * 0.5;
         int s = 0;
@@ -421,7 +438,7 @@ static double compute_max_eig(const double* alphas, const double* betas, int nP)
             xBegin = xn;
         else
             xEnd = xn;
-    } while ((xEnd - xBegin) >= 0.00001);
+    } while ((xEnd - xBegin) >= 0.00001 && ++halvings < 4096);
 #undef T_
     free(p);
     free(T);

@@ -240,3 +240,52 @@ def test_cheby_amg_oracle(orc):
             r = s.b - orc.spmv(s, x)
             assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(s.b)
             A.close()
+
+
+_DEGENERATE_EIGEN = r"""
+import sys
+import numpy as np
+sys.path[:0] = [{root!r}, {tests!r}]
+from oracle_lib import Oracle
+from unap_gb300 import workloads as W
+orc = Oracle("orc")
+out = []
+for s in (W.convdiff(2, 1, 1, seed=3, permute=True, pe=2.0),
+          W.laplace(2, 1, 1, seed=3, permute=True),
+          W.laplace(3, 1, 1, seed=4, permute=True, shift=0.5)):
+    x0 = np.random.default_rng(1).standard_normal(s.n)
+    e, _ = orc.eigen(s, x0, s.b, 10)
+    out.append(e)
+print(repr(out))
+"""
+
+
+def test_eigen_estimate_ends_when_the_diagonal_pcg_stops_early():
+    """The two-cell convection-diffusion system stops the diagonal PCG after
+    two iterations; the reference builds its tridiagonal matrix from all ten
+    (zero alphas, infinite entries) and its bisection never ends.  The
+    oracle's (like the CUDA path's) uses the iterations that ran and returns
+    a finite estimate; the tiny Laplacians beside it end either way.  Run in
+    a child process so that a regression fails instead of stalling the
+    suite."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = _DEGENERATE_EIGEN.format(root=root, tests=os.path.join(root, "tests"))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr[-2000:]
+    vals = eval(r.stdout.strip().splitlines()[-1])
+    assert len(vals) == 3 and all(np.isfinite(v) for v in vals), vals
+
+
+def test_tiny_eigen_estimates_against_reference_library(orc, ref):
+    """Two- and three-cell Laplacians, on which the reference's estimate
+    ends: the oracle's estimate and iterate are the reference's, bit for
+    bit."""
+    for s in (W.laplace(2, 1, 1, seed=3, permute=True),
+              W.laplace(3, 1, 1, seed=4, permute=True, shift=0.5)):
+        x0 = np.random.default_rng(1).standard_normal(s.n)
+        a, xa = orc.eigen(s, x0, s.b, 10)
+        b, xb = ref.eigen(s, x0, s.b, 10)
+        assert a == b and _eq(xa, xb), (a, b)
