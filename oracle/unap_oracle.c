@@ -384,11 +384,12 @@ static void diag_pcg_loops(const omat* m, double* x, const double* b, const doub
 /* computeMaxEig + computeValueForMatrix + determineEigRange + h14Sturm,
  * eigenDiagPCG.cpp:242-361 (tridiagonal Lanczos matrix, Sturm bisection).
  *
- * One departure, on input the reference never finishes: when the diagonal
- * PCG stops early (wArA below VSMALL, e.g. a system of two or three cells
- * solved exactly), the reference still builds the tridiagonal matrix from
- * all nDiagPCGs iterations, the missing alphas are 0, the matrix holds
- * infinities and its bisection never ends.  Here, as in the CUDA path, the
+ * One departure, where the diagonal PCG stops early (wArA below VSMALL:
+ * a one-cell system, a two-cell convection-diffusion system): the
+ * reference still builds the tridiagonal matrix from all nDiagPCGs
+ * iterations, the missing alphas are 0 and the matrix holds infinities;
+ * its bisection then returns an artefact of them (0.99999237 for one cell)
+ * or never ends (the two-cell case).  Here, as in the CUDA path, the
  * matrix stops at the first iteration that did not run (one row: 1 /
  * alpha_0; none: 1) and the bisection at 4096 halvings.  Whenever the
  * diagonal PCG runs all its iterations the result is the reference's, bit

@@ -279,6 +279,18 @@ def test_eigen_estimate_ends_when_the_diagonal_pcg_stops_early():
     assert len(vals) == 3 and all(np.isfinite(v) for v in vals), vals
 
 
+def test_eigen_estimate_of_one_cell_is_one_over_alpha(orc):
+    """A one-cell system: the diagonal PCG solves it in its first iteration
+    (alpha_0 = 1) and stops; the estimate is 1 / alpha_0 from the one
+    iteration that ran (the reference bisects over infinite entries and
+    returns 0.99999237), and the iterate is the exact solution b / d."""
+    s = W.laplace(1, 1, 1, seed=3, permute=True)
+    assert s.n == 1 and s.nf == 0
+    e, x = orc.eigen(s, np.array([0.7]), s.b, 10)
+    assert e == 1.0
+    assert np.allclose(x, s.b / s.diag, rtol=1e-15)
+
+
 def test_tiny_eigen_estimates_against_reference_library(orc, ref):
     """Two- and three-cell Laplacians, on which the reference's estimate
     ends: the oracle's estimate and iterate are the reference's, bit for
