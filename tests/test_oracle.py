@@ -301,3 +301,21 @@ def test_tiny_eigen_estimates_against_reference_library(orc, ref):
         a, xa = orc.eigen(s, x0, s.b, 10)
         b, xb = ref.eigen(s, x0, s.b, 10)
         assert a == b and _eq(xa, xb), (a, b)
+
+
+def test_mg_without_coarse_levels(orc):
+    """A matrix already at or below nCellsCoarsest gets no coarse level (the
+    reference's MGSolver then dereferences a missing level and crashes).
+    The oracle, like the CUDA MgSolver, runs the V-cycle without coarse
+    levels: nothing is prolongated into the finest correction, so without
+    correction scaling Gauss-Seidel MG is plain Gauss-Seidel iteration (with
+    it, the scaling's Jacobi update still acts)."""
+    s = W.laplace(1, 1, 7, seed=5, permute=True, rhs="normal")
+    w = np.abs(s.upper) / np.sqrt(np.sum(s.upper ** 2))
+    assert orc.hierarchy(s, w, n_coarsest=8) == []
+    x, st = orc.mg(s, s.b, w, n_coarsest=8, smoother=1, rel_tol=1e-8, max_iter=3, n_finest=2,
+                   scale_corr=0)
+    assert st["n_levels"] == 0 and st["n_iter"] == 3
+    assert _eq(x, orc.gs(s, np.zeros(s.n), s.b, 6))
+    x, st = orc.mg(s, s.b, w, n_coarsest=8, smoother=1, rel_tol=1e-8, max_iter=40)
+    assert st["n_levels"] == 0 and np.all(np.isfinite(x))
