@@ -38,10 +38,8 @@ def mg_weights(s):
     return np.abs(s.upper) / np.sqrt(np.sum(s.upper ** 2))
 
 
-def main():
-    if not ref_available():
-        raise SystemExit("build the reference first: make -C oracle ref")
-    ref = Oracle("ref")
+def generate(ref):
+    """Every fixture array, computed by the reference library `ref`."""
     out = {}
     for ci, s in enumerate(cases()):
         k = f"c{ci}/"
@@ -87,7 +85,13 @@ def main():
             out[k + f"mg{sm}_x"] = xs
             out[k + f"mg{sm}_stats"] = np.array([st["n_iter"], st["init_res"], st["final_res"],
                                                  st["converged"], st["n_levels"]])
-    np.savez_compressed(OUT, **out)
+    return out
+
+
+def main():
+    if not ref_available():
+        raise SystemExit("build the reference first: make -C oracle ref")
+    np.savez_compressed(OUT, **generate(Oracle("ref")))
     print(f"wrote {OUT} ({os.path.getsize(OUT)} bytes)")
 
 

@@ -342,3 +342,21 @@ def test_tiny_and_thin_systems_against_reference_library(orc, ref, shape):
                 assert _eq(a[0], b[0]) and a[1] == b[1], (gen, shape, t)
             a, b = (o.pbicgstab(s, t, s.b, rel_tol=1e-9, max_iter=200) for o in (orc, ref))
             assert _eq(a[0], b[0]) and a[1] == b[1], (gen, shape, t)
+
+
+def test_golden_fixture_is_what_its_generator_writes(ref):
+    """tests/golden/reference_small.npz holds exactly what
+    tests/golden/make_golden.py computes with the reference library built
+    here: every array, bit for bit."""
+    import importlib.util
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(here, "golden", "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    fresh = mod.generate(ref)
+    with np.load(os.path.join(here, "golden", "reference_small.npz")) as z:
+        assert sorted(z.files) == sorted(fresh)
+        for k in z.files:
+            assert _eq(z[k], fresh[k]), k
